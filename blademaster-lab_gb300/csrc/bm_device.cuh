@@ -1,0 +1,141 @@
+// Device-side helpers shared by the kernels: structure-of-arrays access,
+// stencil lookup, field slots, the float32 tool mirror and the exact 128-bit
+// accumulators.  Every kernel translation unit is compiled with --fmad=false
+// so the arithmetic matches the oracle's operation sequence.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/blademaster_gb300.h"
+#include "bm_scalar.h"
+
+namespace bm {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ bm_v3 ld3(const float* __restrict__ a, int64_t n, int64_t i) {
+    return v3(a[i], a[n + i], a[2 * n + i]);
+}
+__device__ __forceinline__ void st3(float* __restrict__ a, int64_t n, int64_t i, bm_v3 v) {
+    a[i] = v.x;
+    a[n + i] = v.y;
+    a[2 * n + i] = v.z;
+}
+__device__ __forceinline__ bm_m33 ld9(const float* __restrict__ a, int64_t n, int64_t i) {
+    bm_m33 m;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) m.m[r][c] = a[(3 * r + c) * n + i];
+    return m;
+}
+__device__ __forceinline__ void st9(float* __restrict__ a, int64_t n, int64_t i, const bm_m33& m) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a[(3 * r + c) * n + i] = m.m[r][c];
+}
+
+// Node offset of stencil index a = 4 ox + 2 oy + oz (geometry OFFSETS order).
+__device__ __forceinline__ int node_offset(const bm_params& P, int a) {
+    return ((a >> 2) & 1) * P.node_dims[1] * P.node_dims[2] + ((a >> 1) & 1) * P.node_dims[2] + (a & 1);
+}
+__device__ __forceinline__ int field_of(uint64_t fidx, int a) { return (int)((fidx >> (8 * a)) & 0xffu); }
+__device__ __forceinline__ int64_t slot_of(const bm_params& P, int base, uint64_t fidx, int a) {
+    return (int64_t)field_of(fidx, a) * P.node_count + base + node_offset(P, a);
+}
+__device__ __forceinline__ float stencil_w(const bm_buffers& B, int sid, int a) { return __ldg(&B.stencil_w[8 * sid + a]); }
+__device__ __forceinline__ bm_v3 stencil_g(const bm_buffers& B, int sid, int a) {
+    const float* g = B.stencil_g + 24 * sid + 3 * a;
+    return v3(__ldg(g), __ldg(g + 1), __ldg(g + 2));
+}
+
+struct ToolF {
+    bm_v3 pos, vel, omega;
+    bm_q rot;
+};
+__device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
+    ToolF r;
+    r.pos = v3(t[0], t[1], t[2]);
+    r.vel = v3(t[3], t[4], t[5]);
+    r.rot.x = t[6];
+    r.rot.y = t[7];
+    r.rot.z = t[8];
+    r.rot.w = t[9];
+    r.omega = v3(t[10], t[11], t[12]);
+    return r;
+}
+
+// Exact accumulation: warp-sum of 128-bit fixed-point values, then one
+// carry-propagating pair of 64-bit atomics per warp.
+__device__ __forceinline__ bm_fx warp_sum_fx(bm_fx v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        bm_fx o;
+        o.lo = __shfl_xor_sync(0xffffffffu, v.lo, d);
+        o.hi = __shfl_xor_sync(0xffffffffu, v.hi, d);
+        v = bm_fx_add(v, o);
+    }
+    return v;
+}
+__device__ __forceinline__ void atomic_add_fx(uint64_t* acc, bm_fx v) {
+    unsigned long long* lo = reinterpret_cast<unsigned long long*>(acc);
+    unsigned long long* hi = lo + 1;
+    unsigned long long old = atomicAdd(lo, (unsigned long long)v.lo);
+    unsigned long long carry = (old + (unsigned long long)v.lo) < old ? 1ull : 0ull;
+    unsigned long long add_hi = (unsigned long long)v.hi + carry;
+    if (add_hi != 0ull) atomicAdd(hi, add_hi);
+}
+// All 32 lanes must call (values may be zero); lane 0 performs the atomics.
+__device__ __forceinline__ void warp_accumulate(uint64_t* acc, bm_fx v) {
+    v = warp_sum_fx(v);
+    if ((threadIdx.x & 31) == 0 && (v.lo != 0u || v.hi != 0u)) atomic_add_fx(acc, v);
+}
+__device__ __forceinline__ bm_fx fx_zero() {
+    bm_fx z;
+    z.lo = 0u;
+    z.hi = 0u;
+    return z;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(float* addr, float v) {
+    // Non-negative floats order like their bit patterns.
+    atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+}
+
+__device__ __forceinline__ int compatible_masks(uint64_t ones_a, uint64_t twos_a, uint64_t ones_b, uint64_t twos_b) {
+    return (ones_a & twos_b) == 0u && (twos_a & ones_b) == 0u;
+}
+
+// material.compatible (material.py:23-34) on int64 codes.
+__device__ __forceinline__ int compatible_codes(int64_t a, int64_t b) {
+    while (a != 0 || b != 0) {
+        int64_t x = a % 3, y = b % 3;
+        if (x != 0 && y != 0 && x != y) return 0;
+        a /= 3;
+        b /= 3;
+    }
+    return 1;
+}
+
+__device__ __forceinline__ void digit_masks(int64_t code, uint64_t* ones, uint64_t* twos) {
+    uint64_t o = 0u, t = 0u;
+    int bit = 0;
+    while (code != 0) {
+        int64_t d = code % 3;
+        if (d == 1) o |= (uint64_t)1 << bit;
+        if (d == 2) t |= (uint64_t)1 << bit;
+        code /= 3;
+        ++bit;
+    }
+    *ones = o;
+    *twos = t;
+}
+
+inline unsigned grid_for(int64_t count, int block = kBlock) {
+    int64_t g = (count + block - 1) / block;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace bm

@@ -1,0 +1,64 @@
+// Host-side internals shared by the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/blademaster_gb300.h"
+
+struct bm_solver {
+    bm_params P;
+    bm_buffers B;
+    float* viscous_scratch;  // [9][n] inside B.scratch
+    int32_t* scan_partials;  // inside B.scratch
+    int64_t buckets;
+};
+
+namespace bm {
+
+// material
+void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st);
+void launch_material(const bm_solver* s, int write_sums, cudaStream_t st);
+void launch_g2p(const bm_solver* s, cudaStream_t st);
+void launch_remap(const bm_solver* s, cudaStream_t st);
+void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, cudaStream_t st);
+void launch_refresh_stress(const bm_solver* s, cudaStream_t st);
+void launch_validate(const bm_solver* s, cudaStream_t st);
+void launch_clear_flag(const bm_solver* s, int which, cudaStream_t st);
+void launch_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, cudaStream_t st);
+
+// contact
+void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st);
+void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st);
+void launch_pairs(const bm_solver* s, cudaStream_t st);
+void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st);
+void launch_blade_query(const float* local, int n, const float* half, float bevel, float* closest, float* normal,
+                        float* distance, cudaStream_t st);
+void launch_friction(const float* normal, const float* relative, const float* jn, const float* history, int n, float me,
+                     float dt, float mus, float mud, float gk, float gc, float* impulse, float* new_history,
+                     cudaStream_t st);
+void launch_resist_cut(const float* j, const float* x, const float* v, const float* origin, const float* tool_velocity,
+                       const float* q, const float* tool_angular, const float* half, float radius, float spacing,
+                       float* damage, float threshold, int cutting, uint64_t* work_acc, float* result, int n,
+                       cudaStream_t st);
+void launch_assign_only(const bm_solver* s, int cut_index, int cutting, cudaStream_t st);
+
+// tool
+void launch_tool_step(const bm_solver* s, int mode, int target_index, int advance_step, cudaStream_t st);
+void launch_load_external(const bm_solver* s, cudaStream_t st);
+void launch_store_interval(const bm_solver* s, cudaStream_t st);
+void launch_record_pose(const bm_solver* s, int index, cudaStream_t st);
+void launch_tool_mirror(const bm_solver* s, cudaStream_t st);
+void launch_read_acc(const bm_solver* s, float* reaction, float* torque, float* board, float* work, cudaStream_t st);
+void launch_write_acc(const bm_solver* s, const float* reaction, const float* torque, const float* board,
+                      const float* work, cudaStream_t st);
+void launch_step_counter(const bm_solver* s, cudaStream_t st);
+void launch_couple_probe(const int64_t* codes, const float* mass, const float* state, const int32_t* node_start,
+                         int nodes, float* result, cudaStream_t st);
+void launch_g2p_probe(float* x, float* v, const int32_t* slots, const float* weights, const float* old_v,
+                      const float* new_v, int n, float dt, float flip, cudaStream_t st);
+
+// Tool kernel modes.
+enum ToolMode { kToolDrive = 0, kToolFinishExternal = 1, kToolAccumulate = 2, kToolClear = 3 };
+
+}  // namespace bm

@@ -1,0 +1,660 @@
+// Topology-aware TLMPM transfers and constitutive update on the GB300
+// (blademaster_warp/material.py).
+//
+// Layout: particles are sorted by reference cell, so the particles that weigh
+// a grid node are the contents of its eight adjacent cells, contiguous in
+// memory.  The reference scatters (p, a) contributions with float atomics into
+// a hash of (node, code) keys; here every grid slot is produced by one thread
+// that gathers its contributions in ascending particle order, so the sums are
+// deterministic and no float atomic touches the primary fields.  A node's
+// fields (one per distinct cut code among its contributors, ascending code)
+// live at slot f * node_count + node; each particle carries the field index of
+// each of its eight stencil nodes in one uint64 (fidx).
+#include "bm_device.cuh"
+#include "bm_internal.h"
+
+namespace bm {
+
+// Visit the contributions to node n in ascending particle order: adjacent
+// cells in ascending cell index (stencil index a = 7 .. 0), particles of each
+// cell in order.  fn(p, a) is called for each.
+template <typename Fn>
+__device__ __forceinline__ void for_contributions(const bm_params& P, const bm_buffers& B, int n, Fn fn) {
+    const int nyz = P.node_dims[1] * P.node_dims[2];
+    const int i = n / nyz, j = (n / P.node_dims[2]) % P.node_dims[1], k = n % P.node_dims[2];
+#pragma unroll 1
+    for (int a = 7; a >= 0; --a) {
+        const int ci = i - ((a >> 2) & 1), cj = j - ((a >> 1) & 1), ck = k - (a & 1);
+        if (ci < 0 || cj < 0 || ck < 0 || ci >= P.cell_dims[0] || cj >= P.cell_dims[1] || ck >= P.cell_dims[2]) continue;
+        const int c = (ci * P.cell_dims[1] + cj) * P.cell_dims[2] + ck;
+        const int begin = B.cell_start[c], end = B.cell_start[c + 1];
+#pragma unroll 1
+        for (int p = begin; p < end; ++p) fn(p, a);
+    }
+}
+
+// ---------------------------------------------------------------- topology
+
+// Solver._register_topology, node pass: the distinct codes among a node's
+// contributors in ascending order (material.register, material.py:50-66).
+__global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
+    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    int nf = 0;
+    int64_t prev = 0;
+    bool have_prev = false;
+    for (;;) {
+        int64_t best = 0;
+        bool found = false;
+        for_contributions(P, B, n, [&](int p, int) {
+            const int64_t c = field_codes[p];
+            if ((!have_prev || c > prev) && (!found || c < best)) {
+                best = c;
+                found = true;
+            }
+        });
+        if (!found) break;
+        if (nf >= P.fmax) {
+            atomicAdd(&B.errors[0], 1);
+            break;
+        }
+        const int64_t s = (int64_t)nf * P.node_count + n;
+        B.fcode[s] = best;
+        uint64_t ones, twos;
+        digit_masks(best, &ones, &twos);
+        B.fones[s] = ones;
+        B.ftwos[s] = twos;
+        ++nf;
+        prev = best;
+        have_prev = true;
+    }
+    B.nfield[n] = nf;
+}
+
+// Particle pass: the field index of the particle's code at each stencil node.
+__global__ void k_register_particles(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
+    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int64_t code = field_codes[p];
+    const int base = B.base_node[p];
+    uint64_t fidx = 0u;
+    for (int a = 0; a < 8; ++a) {
+        const int node = base + node_offset(P, a);
+        const int nf = B.nfield[node];
+        int f = 0;
+        while (f < nf && B.fcode[(int64_t)f * P.node_count + node] != code) ++f;
+        if (f >= nf) f = 0;  // only after a field overflow, already counted in errors[0]
+        fidx |= (uint64_t)f << (8 * a);
+    }
+    B.fidx[p] = fidx;
+}
+
+__global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
+
+// ------------------------------------------------------------------- P2G
+
+struct NodeSums {
+    float m;
+    bm_v3 mom, J;
+};
+
+// material.p2g (material.py:127-152) for field f of node n, ascending particle order.
+__device__ __forceinline__ NodeSums p2g_sums(const bm_params& P, const bm_buffers& B, int n, int f, bool all) {
+    NodeSums s;
+    s.m = 0.0f;
+    s.mom = v3_zero();
+    s.J = v3_zero();
+    const float dtv = P.dt * P.volume;
+    const int64_t N = P.n;
+    for_contributions(P, B, n, [&](int p, int a) {
+        if (!all && field_of(B.fidx[p], a) != f) return;
+        const int sid = B.stencil_id[p];
+        const float w = stencil_w(B, sid, a);
+        const bm_v3 g = stencil_g(B, sid, a);
+        const float mw = P.mass * w;
+        s.m = s.m + mw;
+        s.mom = v3_add(s.mom, v3_mul(ld3(B.v, N, p), mw));
+        const bm_v3 jp = v3_mul(ld3(B.impulses, N, p), w);
+        const bm_v3 sg = m33_mul_v3(m33_scale(ld9(B.stress, N, p), dtv), g);
+        s.J = v3_add(s.J, v3_sub(jp, sg));
+    });
+    return s;
+}
+
+// p2g + couple_and_velocity (material.py:127-152, 252-284), one thread per
+// active node; also clears the topology flag consumed by registration.
+__global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int64_t S = (int64_t)P.fmax * P.node_count;
+    if (nf == 1) {
+        const NodeSums s = p2g_sums(P, B, n, 0, true);
+        B.grid_mass[n] = s.m;
+        if (write_sums) {
+            st3(B.momentum, S, n, s.mom);
+            st3(B.grid_impulse, S, n, s.J);
+        }
+        if (s.m <= 0.0f) {
+            st3(B.old_v, S, n, v3_zero());
+            st3(B.new_v, S, n, v3_zero());
+            return;
+        }
+        const bm_v3 pm = v3_add(s.mom, v3_div(v3_zero(), s.m));
+        const bm_v3 jm = v3_add(s.J, v3_div(v3_zero(), s.m));
+        st3(B.old_v, S, n, v3_div(pm, s.m));
+        st3(B.new_v, S, n, v3_div(v3_add(pm, jm), s.m));
+        return;
+    }
+    for (int f = 0; f < nf; ++f) {
+        const NodeSums s = p2g_sums(P, B, n, f, false);
+        const int64_t slot = (int64_t)f * P.node_count + n;
+        B.grid_mass[slot] = s.m;
+        st3(B.momentum, S, slot, s.mom);
+        st3(B.grid_impulse, S, slot, s.J);
+    }
+    for (int f = 0; f < nf; ++f) {
+        const int64_t a = (int64_t)f * P.node_count + n;
+        const float ma = B.grid_mass[a];
+        if (ma <= 0.0f) {
+            st3(B.old_v, S, a, v3_zero());
+            st3(B.new_v, S, a, v3_zero());
+            continue;
+        }
+        const bm_v3 pa = ld3(B.momentum, S, a), ja = ld3(B.grid_impulse, S, a);
+        const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+        float total = 0.0f;
+        bm_v3 dm = v3_zero(), di = v3_zero();
+        for (int g = 0; g < nf; ++g) {
+            const int64_t b = (int64_t)g * P.node_count + n;
+            const float mb = B.grid_mass[b];
+            total = total + mb;
+            if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b])) {
+                dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, b), ma), v3_mul(pa, mb)));
+                di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, b), ma), v3_mul(ja, mb)));
+            }
+        }
+        const bm_v3 pm = v3_add(pa, v3_div(dm, total));
+        const bm_v3 jm = v3_add(ja, v3_div(di, total));
+        st3(B.old_v, S, a, v3_div(pm, ma));
+        st3(B.new_v, S, a, v3_div(v3_add(pm, jm), ma));
+    }
+}
+
+// ------------------------------------------------------------------- G2P
+
+// material.g2p_at (material.py:343-367) plus the pair-list displacement check
+// of contact.check_pair_list (contact.py:716-735) on the new x, v.
+__global__ void k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int sid = B.stencil_id[p], base = B.base_node[p];
+    const uint64_t fidx = B.fidx[p];
+    bm_v3 pic = v3_zero(), dv = v3_zero();
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const int64_t s = slot_of(P, base, fidx, a);
+        const float w = stencil_w(B, sid, a);
+        const bm_v3 nv = ld3(B.new_v, S, s);
+        pic = v3_add(pic, v3_mul(nv, w));
+        dv = v3_add(dv, v3_mul(v3_sub(nv, ld3(B.old_v, S, s)), w));
+    }
+    const bm_v3 v = v3_add(v3_mul(pic, 1.0f - P.flip), v3_mul(v3_add(ld3(B.v, N, p), dv), P.flip));
+    const bm_v3 x = v3_add(ld3(B.x, N, p), v3_mul(pic, P.dt));
+    st3(B.v, N, p, v);
+    st3(B.x, N, p, x);
+    if (check_list) {
+        if (v3_len(v3_sub(x, ld3(B.built_x, N, p))) + P.dt * v3_len(v) > half_skin) B.flags[BM_FLAG_PAIR_DIRTY] = 1;
+    }
+}
+
+// ---------------------------------------------------------- remap + couple
+
+// The MUSL re-scatter of g2p_remap (material.py:397-401) gathered per slot,
+// then couple (material.py:155-193); stores coupled / mass for the F update.
+__global__ void k_remap_couple(bm_params P, bm_buffers B) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    if (nf == 1) {
+        bm_v3 r = v3_zero();
+        for_contributions(P, B, n, [&](int p, int a) {
+            r = v3_add(r, v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a)));
+        });
+        const float m = B.grid_mass[n];
+        if (m <= 0.0f) {
+            st3(B.remap_v, S, n, v3_zero());
+            return;
+        }
+        const bm_v3 coupled = v3_add(r, v3_div(v3_zero(), m));
+        st3(B.remap_v, S, n, v3_div(coupled, m));
+        return;
+    }
+    for (int f = 0; f < nf; ++f) {
+        bm_v3 r = v3_zero();
+        for_contributions(P, B, n, [&](int p, int a) {
+            if (field_of(B.fidx[p], a) != f) return;
+            r = v3_add(r, v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a)));
+        });
+        st3(B.remapped, S, (int64_t)f * P.node_count + n, r);
+    }
+    for (int f = 0; f < nf; ++f) {
+        const int64_t a = (int64_t)f * P.node_count + n;
+        const float ma = B.grid_mass[a];
+        if (ma <= 0.0f) {
+            st3(B.remap_v, S, a, v3_zero());
+            continue;
+        }
+        const bm_v3 sa = ld3(B.remapped, S, a);
+        const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+        float total = 0.0f;
+        bm_v3 ex = v3_zero();
+        for (int g = 0; g < nf; ++g) {
+            const int64_t b = (int64_t)g * P.node_count + n;
+            const float mb = B.grid_mass[b];
+            total = total + mb;
+            if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
+                ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, b), ma), v3_mul(sa, mb)));
+        }
+        st3(B.remap_v, S, a, v3_div(v3_add(sa, v3_div(ex, total)), ma));
+    }
+}
+
+// ---------------------------------------------------------- constitutive
+
+// Fixed-corotated first Piola stress through the polar rotation:
+// P = 2 mu (f - R) + lam (J - 1) J f^-T, equal to material.corotated_stress
+// (material.py:78-91) with Fp = I.
+__device__ __forceinline__ bm_m33 corotated_polar(const bm_m33& f, float J, float mu, float lam) {
+    const bm_m33 R = bm_polar3(f);
+    const bm_m33 inv_t = m33_transpose(m33_inverse(f));
+    const float c = lam * (J - 1.0f) * J, two_mu = 2.0f * mu;
+    bm_m33 out;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) out.m[i][j] = two_mu * (f.m[i][j] - R.m[i][j]) + c * inv_t.m[i][j];
+    return out;
+}
+
+__device__ bm_m33 corotated_svd(const bm_m33& U, bm_v3 s, const bm_m33& V, const bm_m33& plastic_inverse, float mu,
+                                float lam) {
+    const float J = (s.x * s.y) * s.z;
+    bm_v3 d;
+    for (int i = 0; i < 3; ++i) {
+        const float si = v3_get(s, i);
+        v3_set(&d, i, 2.0f * mu * (si - 1.0f) + lam * (J - 1.0f) * J / si);
+    }
+    return m33_mul(m33_mul(m33_mul(U, m33_diag(d)), m33_transpose(V)), m33_transpose(plastic_inverse));
+}
+
+// material.stress_at (material.py:94-112).
+__device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
+    const int64_t N = P.n;
+    const bm_m33 F = ld9(B.F, N, p);
+    bm_m33 f = F, pinv = m33_identity();
+    if (P.use_fp) {
+        pinv = m33_inverse(ld9(B.Fp, N, p));
+        f = m33_mul(F, pinv);
+    }
+    const float J = m33_det(f);
+    if (J <= 0.0f || !bm_isfinitef(J)) {
+        atomicAdd(&B.errors[1], 1);
+        st9(B.stress, N, p, m33_zero());
+        return;
+    }
+    if (P.use_fp) st9(B.stress, N, p, m33_mul(corotated_polar(f, J, P.mu, P.lam), m33_transpose(pinv)));
+    else st9(B.stress, N, p, corotated_polar(f, J, P.mu, P.lam));
+}
+
+// material.plastic_at (material.py:404-431).
+__device__ bool plastic_at(const bm_params& P, const bm_buffers& B, int p, float yield_stress, bm_m33* U, bm_v3* s,
+                           bm_m33* V) {
+    const int64_t N = P.n;
+    const bm_m33 F = ld9(B.F, N, p);
+    bm_svd3(m33_mul(F, m33_inverse(ld9(B.Fp, N, p))), U, s, V);
+    if (bm_minf(bm_minf(s->x, s->y), s->z) <= 0.0f) {
+        atomicAdd(&B.errors[1], 1);
+        return false;
+    }
+    const bm_v3 e = v3(bm_logf(s->x), bm_logf(s->y), bm_logf(s->z));
+    const float mean = ((e.x + e.y) + e.z) / 3.0f;
+    const bm_v3 dev = v3_sub(e, v3(mean, mean, mean));
+    const float norm = v3_len(dev);
+    const float limit = yield_stress / (2.0f * P.mu) * sqrtf(2.0f / 3.0f);
+    if (norm > limit) {
+        const bm_v3 ep = v3_sub(e, v3_mul(dev, 1.0f - limit / norm));
+        *s = v3(bm_expf(ep.x), bm_expf(ep.y), bm_expf(ep.z));
+        const bm_m33 next_f = m33_mul(m33_mul(*U, m33_diag(*s)), m33_transpose(*V));
+        st9(B.Fp, N, p, m33_mul(m33_inverse(next_f), F));
+    }
+    return true;
+}
+
+// material.maxwell_at (material.py:485-533).
+__device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const bm_m33& U, bm_v3 sigma,
+                           const bm_m33& V, float relax) {
+    const int64_t N = P.n;
+    const bm_m33 f = m33_mul(m33_mul(U, m33_diag(sigma)), m33_transpose(V));
+    double D[9];
+    for (int r = 0; r < 9; ++r) D[r] = B.viscous[(int64_t)r * N + p];
+    bm_m33 Df;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Df.m[r][c] = (float)D[3 * r + c];
+    const bm_m33 fm = m33_mul(f, m33_inverse(m33_add(m33_identity(), Df)));
+    bm_m33 Um, Vm;
+    bm_v3 sm;
+    bm_svd3(fm, &Um, &sm, &Vm);
+    if (bm_minf(bm_minf(sm.x, sm.y), sm.z) <= 0.0f) {
+        atomicAdd(&B.errors[1], 1);
+        st9(B.stress, N, p, m33_zero());
+        return;
+    }
+    const bm_v3 e = v3(bm_logf(sm.x), bm_logf(sm.y), bm_logf(sm.z));
+    const float mean = ((e.x + e.y) + e.z) / 3.0f;
+    bm_v3 dev = v3_sub(e, v3(mean, mean, mean));
+    if (relax > 0.0f) {
+        const bm_v3 step = v3_mul(dev, relax);
+        dev = v3_sub(dev, step);
+        const bm_v3 growth = v3(bm_expm1f(-step.x), bm_expm1f(-step.y), bm_expm1f(-step.z));
+        const bm_m33 delta = m33_mul(m33_mul(Vm, m33_diag(growth)), m33_transpose(Vm));
+        double dd[9], nd[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) dd[3 * r + c] = (double)delta.m[r][c];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double prod = 0.0;
+                for (int k = 0; k < 3; ++k) prod = prod + dd[3 * r + k] * D[3 * k + c];
+                nd[3 * r + c] = (D[3 * r + c] + dd[3 * r + c]) + prod;
+            }
+        for (int r = 0; r < 9; ++r) B.viscous[(int64_t)r * N + p] = nd[r];
+    }
+    const bm_m33 kirchhoff = m33_mul(m33_mul(Um, m33_diag(v3_mul(dev, 2.0f * P.mu_maxwell))), m33_transpose(Um));
+    const float mu_eq = P.mu - P.mu_maxwell;
+    const float lam_eq = P.lam + 2.0f / 3.0f * P.mu_maxwell;
+    const bm_m33 equilibrium = corotated_svd(U, sigma, V, m33_inverse(ld9(B.Fp, N, p)), mu_eq, lam_eq);
+    st9(B.stress, N, p, m33_add(equilibrium, m33_mul(kirchhoff, m33_transpose(m33_inverse(ld9(B.F, N, p))))));
+}
+
+// material.maxwell_stress_at (material.py:536-566).
+__device__ void maxwell_stress_at(const bm_params& P, const bm_buffers& B, int p, float relax) {
+    const int64_t N = P.n;
+    bm_m33 U, V;
+    bm_v3 sigma;
+    if (P.yield_stress > 0.0f) {
+        if (!plastic_at(P, B, p, P.yield_stress, &U, &sigma, &V)) {
+            st9(B.stress, N, p, m33_zero());
+            return;
+        }
+        maxwell_at(P, B, p, U, sigma, V, relax);
+        return;
+    }
+    const bm_m33 f = m33_mul(ld9(B.F, N, p), m33_inverse(ld9(B.Fp, N, p)));
+    const float J = m33_det(f);
+    if (J <= 0.0f || !bm_isfinitef(J)) {
+        atomicAdd(&B.errors[1], 1);
+        st9(B.stress, N, p, m33_zero());
+        return;
+    }
+    bm_svd3(f, &U, &sigma, &V);
+    maxwell_at(P, B, p, U, sigma, V, relax);
+}
+
+__device__ void constitutive(const bm_params& P, const bm_buffers& B, int p) {
+    if (P.maxwell) {
+        maxwell_stress_at(P, B, p, P.maxwell_relax);
+    } else if (P.plastic) {
+        bm_m33 U, V;
+        bm_v3 s;
+        if (plastic_at(P, B, p, P.yield_stress, &U, &s, &V))
+            st9(B.stress, P.n, p, corotated_svd(U, s, V, m33_inverse(ld9(B.Fp, P.n, p)), P.mu, P.lam));
+        else
+            st9(B.stress, P.n, p, m33_zero());
+    } else {
+        stress_at(P, B, p);
+    }
+}
+
+// material.compute_stress / compute_stress_maxwell (material.py:115-124, 569-589).
+__global__ void k_refresh_stress(bm_params P, bm_buffers B) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    if (P.maxwell) maxwell_stress_at(P, B, p, 0.0f);
+    else stress_at(P, B, p);
+}
+
+// material.plastic_project (material.py:434-442) on caller arrays.
+__global__ void k_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    bm_params P = {};
+    P.n = n;
+    P.mu = mu;
+    bm_buffers B = {};
+    B.F = F;
+    B.Fp = Fp;
+    B.errors = errors;
+    bm_m33 U, V;
+    bm_v3 s;
+    plastic_at(P, B, p, yield_stress, &U, &s, &V);
+}
+
+// contact.assign (contact.py:996-1039) for every knife, knife k labelling the
+// digit 3^(cut_index + k).
+__device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int cut_index, int cutting) {
+    if (cutting == 0) return;
+    const int64_t N = P.n;
+    const bm_v3 xp = ld3(B.x, N, p), vp = ld3(B.v, N, p);
+    int64_t code = B.codes[p];
+    bool changed = false;
+    int64_t digit = 1;
+    for (int e = 0; e < cut_index; ++e) digit *= 3;
+    for (int k = 0; k < P.tool_count; ++k, digit *= 3) {
+        if ((code / digit) % 3 != 0) continue;
+        const ToolF T = load_tool(B.tool_f + 13 * k);
+        const bm_v3 edge = v3_add(T.pos, q_rotate(T.rot, v3(0.0f, 0.0f, -P.half[2])));
+        const bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, edge));
+        const float front = -local.z;
+        const bm_v3 edge_v = v3_add(T.vel, v3_cross(T.omega, v3_sub(edge, T.pos)));
+        const bm_v3 d = q_rotate(T.rot, v3(0.0f, 0.0f, -1.0f));
+        const float advance = v3_dot(v3_sub(edge_v, vp), d);
+        const float back = 2.0f * P.spacing + bm_maxf(advance * P.dt, 0.0f);
+        const bool behind = front >= -back && front <= 0.0f;
+        const bool on_board = (P.board_half[0] == 0.0f || fabsf(xp.x) <= P.board_half[0]) &&
+                              (P.board_half[1] == 0.0f || fabsf(xp.y) <= P.board_half[1]);
+        const bm_v3 edge_here = v3_add(edge, q_rotate(T.rot, v3(0.0f, local.y, 0.0f)));
+        const bool pinched = on_board && edge_here.z <= P.radius && xp.z <= edge_here.z + P.radius;
+        if (fabsf(local.x) <= 6.0f * P.spacing && fabsf(local.y) <= P.half[1] && (behind || pinched)) {
+            code += digit * (local.x < 0.0f ? 1 : 2);
+            changed = true;
+        }
+    }
+    if (changed) {
+        B.codes[p] = code;
+        B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 1;
+        B.flags[BM_FLAG_PAIR_DIRTY] = 1;
+    }
+}
+
+// update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
+// with this substep's side labelling (run after the tool update).
+__global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    if (do_update) {
+        const int sid = B.stencil_id[p], base = B.base_node[p];
+        const uint64_t fidx = B.fidx[p];
+        bm_m33 rate = m33_zero();
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int64_t s = slot_of(P, base, fidx, a);
+            if (B.grid_mass[s] > 0.0f) rate = m33_add(rate, m33_outer(ld3(B.remap_v, S, s), stencil_g(B, sid, a)));
+        }
+        st9(B.F, N, p, m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt)));
+        constitutive(P, B, p);
+    }
+    assign_sides(P, B, p, cut_index, cutting);
+}
+
+// material.validate_interval (material.py:6-20).
+__global__ void k_validate(bm_params P, bm_buffers B) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int64_t N = P.n;
+    const float d = m33_det(ld9(B.F, N, p));
+    int bad = (d <= 0.0f || !bm_isfinitef(d)) ? 1 : 0;
+    for (int i = 0; i < 3; ++i) {
+        if (!bm_isfinitef(B.x[(int64_t)i * N + p])) ++bad;
+        if (!bm_isfinitef(B.v[(int64_t)i * N + p])) ++bad;
+    }
+    if (bad) atomicAdd(&B.errors[1], bad);
+}
+
+// viscous_impulse (material.py:321-340): per-particle viscous stress, then a
+// per-slot gather added to grid_impulse in ascending particle order.
+__global__ void k_viscous_stress(bm_params P, bm_buffers B, float* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int sid = B.stencil_id[p], base = B.base_node[p];
+    const uint64_t fidx = B.fidx[p];
+    bm_m33 rate = m33_zero();
+    for (int a = 0; a < 8; ++a)
+        rate = m33_add(rate, m33_outer(ld3(B.old_v, S, slot_of(P, base, fidx, a)), stencil_g(B, sid, a)));
+    const bm_m33 F = ld9(B.F, N, p);
+    const bm_m33 inv = m33_inverse(F);
+    const bm_m33 L = m33_mul(rate, inv);
+    st9(out, N, p, m33_mul(m33_scale(m33_add(L, m33_transpose(L)), P.dynamic_viscosity * m33_det(F)), m33_transpose(inv)));
+}
+
+__global__ void k_viscous_gather(bm_params P, bm_buffers B, const float* __restrict__ vstress) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const float scale = -P.dt * P.volume;
+    for (int f = 0; f < nf; ++f) {
+        const int64_t slot = (int64_t)f * P.node_count + n;
+        bm_v3 J = ld3(B.grid_impulse, S, slot);
+        for_contributions(P, B, n, [&](int p, int a) {
+            if (field_of(B.fidx[p], a) != f) return;
+            J = v3_add(J, m33_mul_v3(m33_scale(ld9(vstress, N, p), scale), stencil_g(B, B.stencil_id[p], a)));
+        });
+        st3(B.grid_impulse, S, slot, J);
+    }
+}
+
+// couple (material.py:155-193) of `state` into `result` and grid_vel
+// (material.py:212-249) on every field of every active node.  mode 0: couple
+// state -> result; mode 1: old/new velocity from momentum `state` and
+// impulse `result`.
+__global__ void k_couple_slots(bm_params P, bm_buffers B, const float* __restrict__ state, float* __restrict__ result) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int64_t S = (int64_t)P.fmax * P.node_count;
+    for (int f = 0; f < nf; ++f) {
+        const int64_t a = (int64_t)f * P.node_count + n;
+        const float ma = B.grid_mass[a];
+        if (ma <= 0.0f) continue;
+        const bm_v3 sa = ld3(state, S, a);
+        const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+        float total = 0.0f;
+        bm_v3 ex = v3_zero();
+        for (int g = 0; g < nf; ++g) {
+            const int64_t b = (int64_t)g * P.node_count + n;
+            const float mb = B.grid_mass[b];
+            total = total + mb;
+            if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
+                ex = v3_add(ex, v3_sub(v3_mul(ld3(state, S, b), ma), v3_mul(sa, mb)));
+        }
+        st3(result, S, a, v3_add(sa, v3_div(ex, total)));
+    }
+}
+
+__global__ void k_grid_vel(bm_params P, bm_buffers B, const float* __restrict__ momentum, const float* __restrict__ impulse) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int64_t S = (int64_t)P.fmax * P.node_count;
+    for (int f = 0; f < nf; ++f) {
+        const int64_t s = (int64_t)f * P.node_count + n;
+        const float m = B.grid_mass[s];
+        if (m > 0.0f) {
+            const bm_v3 pm = ld3(momentum, S, s);
+            st3(B.old_v, S, s, v3_div(pm, m));
+            st3(B.new_v, S, s, v3_div(v3_add(pm, ld3(impulse, S, s)), m));
+        }
+    }
+}
+
+// --------------------------------------------------------------- launches
+
+void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st) {
+    const bm_params& P = s->P;
+    k_register_nodes<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B, field_codes, force);
+    k_register_particles<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, field_codes, force);
+}
+
+void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
+    const bm_params& P = s->P;
+    const bm_buffers& B = s->B;
+    const int64_t S = (int64_t)P.fmax * P.node_count;
+    if (P.viscous) {
+        // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
+        k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, 1);
+        k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
+        k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.grid_impulse);
+        k_viscous_stress<<<grid_for(P.n), kBlock, 0, st>>>(P, B, s->viscous_scratch);
+        k_viscous_gather<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, s->viscous_scratch);
+        // coupled impulse into remap_v as scratch (overwritten by the remap below)
+        k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.grid_impulse, B.remap_v);
+        k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.remap_v);
+        (void)S;
+    } else {
+        k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, write_sums);
+    }
+}
+
+void launch_g2p(const bm_solver* s, cudaStream_t st) {
+    const bm_params& P = s->P;
+    k_g2p<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
+}
+
+void launch_remap(const bm_solver* s, cudaStream_t st) {
+    const bm_params& P = s->P;
+    k_remap_couple<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B);
+}
+
+void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, cudaStream_t st) {
+    const bm_params& P = s->P;
+    k_fupdate_assign<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, do_update, cut_index, cutting);
+}
+
+void launch_refresh_stress(const bm_solver* s, cudaStream_t st) {
+    k_refresh_stress<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B);
+}
+
+void launch_validate(const bm_solver* s, cudaStream_t st) {
+    k_validate<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B);
+}
+
+void launch_clear_flag(const bm_solver* s, int which, cudaStream_t st) { k_clear_flag<<<1, 1, 0, st>>>(s->B, which); }
+
+void launch_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, cudaStream_t st) {
+    k_plastic_project<<<grid_for(n), kBlock, 0, st>>>(F, Fp, n, mu, yield_stress, errors);
+}
+
+}  // namespace bm

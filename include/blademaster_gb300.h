@@ -1,0 +1,271 @@
+/*
+ * blademaster_gb300 C-ABI: the material substep of BladeMaster-Lab's TLMPM
+ * cutting solver on one GB300 (sm_103a).
+ *
+ * The reference (Ju6276/BladeMaster-Lab, Python + NVIDIA Warp) has no C
+ * interface: its hot path is a fixed sequence of Warp kernel launches driven
+ * by blademaster_warp/solver.py.  Each entry point below replaces one of those
+ * launches (or one Solver method that launches several), named after it, and
+ * is what a host binding (ctypes here, or cgo / JNI / N-API) calls.
+ *
+ * Ownership: every device buffer is allocated by the caller (PyTorch on the
+ * Python side) and passed once in bm_buffers; addresses must stay valid and
+ * fixed for the solver's lifetime, because captured CUDA graphs embed them
+ * (the reference relies on the same rule, solver.py:986-990).  No entry point
+ * allocates device memory except bm_graph_create (graph objects).
+ *
+ * Errors: every function returns 0 on success or a BM_ERR_* class; the
+ * message of the last failure on the calling thread is bm_last_error().
+ * Device-detected errors are counted in buffers.errors[3] = [storage
+ * overflow, inverted material, coincident proxies], the reference's counters
+ * (solver.py:307, raised at solver.py:1022-1026).
+ *
+ * Threading: a solver is driven from one host thread on one stream at a time
+ * (solver.py:158-162 has the same contract).
+ */
+#ifndef BLADEMASTER_GB300_H
+#define BLADEMASTER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BM_OK 0
+#define BM_ERR_ARGUMENT 1
+#define BM_ERR_CUDA 2
+#define BM_ERR_STATE 3
+
+/* Bits of the `cutting` argument (contact.py:15-18). */
+#define BM_CUT_ON 1
+#define BM_CUT_ADVANCE 2
+#define BM_CUT_HOLD 4
+
+#define BM_MAX_TOOLS 16
+#define BM_PAIR_LANES 64
+
+/* Scalars of one solver: Config (solver.py:12-149) plus the derived
+ * constants of Solver.__init__ (solver.py:164-200).  float fields are the
+ * float32 values the particle kernels use; *_d fields are float64 copies used
+ * by the single-thread tool integration. */
+typedef struct bm_params {
+    int32_t n;                 /* particles */
+    int32_t node_count;        /* nodes of the reference grid, prod(cells + 1) */
+    int32_t node_dims[3];
+    int32_t cell_dims[3];
+    int32_t active_nodes;      /* nodes touched by at least one particle */
+    int32_t fmax;              /* field slots per node (slot = f * node_count + node) */
+    int32_t stencil_rows;      /* rows of the stencil table */
+    int32_t tool_count;
+    int32_t pair_capacity;     /* friction-history hash table size (power of two) */
+    int32_t bucket_mask;       /* pair search buckets - 1 (power of two) */
+    int32_t candidate_capacity;
+    /* mode flags */
+    int32_t tool_model;        /* -1 external, 0 guided, 1 free/servo (solver.py:571-576) */
+    int32_t external_tool;
+    int32_t predict;           /* tool_substep == predict */
+    int32_t free_blade;
+    int32_t lock_rotation;     /* guided knife: not free and not pose servo */
+    int32_t accumulate_tool_impulses;
+    int32_t plastic;           /* yield_stress > 0 */
+    int32_t use_fp;            /* Fp may differ from identity */
+    int32_t maxwell;
+    int32_t viscous;           /* dynamic_viscosity > 0 */
+    int32_t pair_search;       /* 0 skin list rebuilt on demand, 1 rebuilt every substep */
+    int32_t cache_topology;    /* register fields only when a cut code changed */
+    /* material */
+    float dt, spacing, mass, volume, radius, mu, lam, mu_maxwell, maxwell_relax;
+    float yield_stress, flip, dynamic_viscosity;
+    /* contact */
+    float normal_scale, tangent_stiffness, friction_static, friction_dynamic, tangent_damping;
+    float board_scale, board_half[2];
+    float half[3], bevel, blade_offset, blade_mass, inertia_inv[3], threshold;
+    float pair_skin, pad1;
+    /* tool drive, float64 */
+    double dt_d, blade_mass_d, half_d[3], bevel_d, inertia_inv_d[3];
+    double drive_stiffness, drive_damping, drive_force_limit, rot_stiffness, rot_damping, friction_dynamic_d;
+    double board_half_d[2];
+} bm_params;
+
+/* Device buffers (caller-owned).  Particle arrays are in device order
+ * (sorted by reference cell) and structure-of-arrays: a "[3][n]" array holds
+ * all x components, then all y, then all z. */
+typedef struct bm_buffers {
+    /* particles */
+    float* x;            /* [3][n] */
+    float* v;            /* [3][n] */
+    float* ref;          /* [3][n] reference positions */
+    float* F;            /* [9][n] row-major components */
+    float* Fp;           /* [9][n] */
+    float* stress;       /* [9][n] first Piola stress of the current F, Fp */
+    double* viscous;     /* [9][n] Fv - I of the Maxwell branch */
+    int64_t* codes;      /* [n] ternary cut codes */
+    int64_t* zero_codes; /* [n] all zero: transfers of the single-field baseline */
+    float* damage;       /* [tools][n] */
+    float* histories;    /* [1 + tools][3][n]: row 0 board, row 1 + k knife k */
+    float* impulses;     /* [3][n] contact impulses of this substep */
+    int32_t* stencil_id; /* [n] row of the stencil table */
+    float* stencil_w;    /* [rows][8] */
+    float* stencil_g;    /* [rows][8][3] */
+    int32_t* base_node;  /* [n] node of the particle's cell corner (0, 0, 0) */
+    uint64_t* fidx;      /* [n] 8 x 8-bit field index of each stencil node */
+    /* grid */
+    int32_t* cell_start; /* [cells + 1] particles of cell c are [cell_start[c], cell_start[c+1]) */
+    int32_t* active;     /* [active_nodes] node ids */
+    int32_t* nfield;     /* [node_count] fields registered at each node */
+    int64_t* fcode;      /* [fmax][node_count] code of each field (ascending per node) */
+    uint64_t* fones;     /* [fmax][node_count] digit masks of the code */
+    uint64_t* ftwos;     /* [fmax][node_count] */
+    float* grid_mass;    /* [fmax * node_count] */
+    float* momentum;     /* [3][fmax * node_count] */
+    float* grid_impulse; /* [3][fmax * node_count] */
+    float* old_v;        /* [3][fmax * node_count] */
+    float* new_v;        /* [3][fmax * node_count] */
+    float* remapped;     /* [3][fmax * node_count] remapped momentum (multi-field nodes) */
+    float* remap_v;      /* [3][fmax * node_count] coupled remapped momentum / mass */
+    /* pair contact */
+    float* built_x;      /* [3][n] */
+    int64_t* built_codes;/* [n] */
+    int32_t* partners;   /* [n][BM_PAIR_LANES] */
+    int32_t* partner_count; /* [n]; -1 overflow */
+    int32_t* candidates; /* [candidate_capacity] particles with partners */
+    int32_t* bucket_start;  /* [buckets + 1] */
+    int32_t* bucket_items;  /* [n] */
+    int32_t* bucket_fill;   /* [buckets] */
+    int32_t* particle_bucket; /* [n] */
+    int64_t* pair_keys;  /* [2][pair_capacity] */
+    float* pair_history; /* [2][pair_capacity][3] */
+    int32_t* pair_used;  /* [2][pair_capacity] */
+    int32_t* pair_count; /* [2] */
+    /* tool and scalar state */
+    double* tool;        /* [tools][13]: pos 3, vel 3, rot xyzw 4, omega 3 */
+    float* tool_f;       /* [tools][13] float32 mirror read by particle kernels */
+    float* mobility;     /* [36] */
+    uint64_t* acc;       /* 128-bit accumulators, see BM_ACC_* */
+    double* interval;    /* [6] interval impulse 3, angular impulse about the world origin 3 */
+    double* table_impulse; /* [tools][3] */
+    float* speed;        /* [1] max particle speed this substep */
+    int32_t* errors;     /* [3] */
+    int32_t* flags;      /* see BM_FLAG_* */
+    float* targets;      /* [steps][3] per-substep edge targets (driven knives) */
+    float* rotations;    /* [steps][4] per-substep target orientations */
+    float* packed;       /* [49] external tool state */
+    float* result;       /* [10 + 7 * samples] interval result */
+    int32_t* scratch;    /* [scratch_len] scan workspace */
+} bm_buffers;
+
+/* Layout of buffers.acc: pairs of uint64 (lo, hi), 2^-96 fixed point. */
+#define BM_ACC_REACTION(k) (2 * (3 * (k)))          /* knife k: 3 components */
+#define BM_ACC_TORQUE(k) (2 * (3 * BM_MAX_TOOLS + 3 * (k)))
+#define BM_ACC_BOARD (2 * (6 * BM_MAX_TOOLS))
+#define BM_ACC_WORK (2 * (6 * BM_MAX_TOOLS + 3))
+#define BM_ACC_WORDS (2 * (6 * BM_MAX_TOOLS + 4))
+
+/* Layout of buffers.flags. */
+#define BM_FLAG_TOPOLOGY_DIRTY 0
+#define BM_FLAG_PAIR_DIRTY 1
+#define BM_FLAG_PAIR_BUILDS 2
+#define BM_FLAG_STEP 3           /* substep counter (history ping-pong parity) */
+#define BM_FLAG_CANDIDATES 4     /* number of pair candidates */
+#define BM_FLAG_EMBEDDED 5       /* count_embedded result */
+#define BM_FLAG_SLOTS 6          /* registered slots */
+#define BM_FLAG_WORDS 8
+
+typedef struct bm_solver bm_solver;
+typedef struct bm_graph bm_graph;
+
+/* Per-substep arguments of one batch of substeps (Solver._step_kernels,
+ * solver.py:920-940). */
+typedef struct bm_step_args {
+    int32_t steps;         /* substeps in the batch */
+    int32_t cut_bits;      /* BM_CUT_* bits, 0 when not cutting */
+    int32_t cut_index;     /* digit of knife k is 3^(cut_index + k) */
+    int32_t single_field;  /* transfers ignore cut codes (solver.py:382-389) */
+    int32_t use_targets;   /* driven knife reads targets/rotations[i] */
+    int32_t external_load; /* prepend load_external_state (coupling.py:118-131) */
+    int32_t external_finish; /* append validate_interval + store_interval (coupling.py:132-136) */
+    int32_t record_samples; /* 0, or samples of record_pose (coupling.py:139-147) */
+    int32_t hold_pose;     /* record only first and last pose (hold mode) */
+    int32_t pad;
+} bm_step_args;
+
+/* Size of the structs as compiled into the library (binding check). */
+uint32_t bm_params_size(void);
+uint32_t bm_buffers_size(void);
+uint32_t bm_step_args_size(void);
+const char* bm_last_error(void);
+const char* bm_version(void);
+/* Number of int32 words of buffers.scratch a solver with these params needs. */
+int64_t bm_scratch_words(const bm_params* params);
+
+/* Solver.__init__ (solver.py:157-316): checks the parameters and binds the buffers. */
+int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solver** out);
+int bm_solver_destroy(bm_solver* solver);
+
+/* Solver.refresh_stress / material.compute_stress (solver.py:318-329, material.py:115-124). */
+int bm_refresh_stress(bm_solver* s, void* stream);
+/* Solver._register_topology (solver.py:391-429): (node, code) fields of every stencil node. */
+int bm_register_topology(bm_solver* s, int single_field, void* stream);
+/* Solver.material_step (solver.py:334-376): P2G, exchange, G2P + remap, F update. */
+int bm_material_step(bm_solver* s, int single_field, void* stream);
+/* Solver.rigid_contacts (solver.py:588-668): gravity, board and every knife. */
+int bm_rigid_contacts(bm_solver* s, int cut_bits, void* stream);
+/* Solver.particle_contacts (solver.py:670-751): pair contact with friction history. */
+int bm_particle_contacts(bm_solver* s, void* stream);
+/* Solver.assign_sides (solver.py:866-890). */
+int bm_assign_sides(bm_solver* s, int cut_index, int cutting, void* stream);
+/* Solver._drive_tool (solver.py:824-864): targets/rotations row `index`. */
+int bm_drive_tool(bm_solver* s, int index, void* stream);
+/* Solver._finish_external_tool / _accumulate_tool_impulses (solver.py:788-822). */
+int bm_finish_external(bm_solver* s, void* stream);
+int bm_accumulate_tool_impulses(bm_solver* s, void* stream);
+/* contact.clear_step (contact.py:1058-1068) for every knife. */
+int bm_clear_step(bm_solver* s, void* stream);
+/* One batch of substeps, launched eagerly on `stream`. */
+int bm_substeps(bm_solver* s, const bm_step_args* args, void* stream);
+/* The same batch captured once as a CUDA graph (Solver.prepare, solver.py:975-1019). */
+int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_graph** out);
+int bm_graph_launch(bm_graph* g, void* stream);
+int bm_graph_destroy(bm_graph* g);
+/* contact.count_embedded (contact.py:1042-1055) into flags[BM_FLAG_EMBEDDED]. */
+int bm_count_embedded(bm_solver* s, int reset, void* stream);
+/* material.validate_interval (material.py:6-20). */
+int bm_validate_interval(bm_solver* s, void* stream);
+/* Convert the 128-bit accumulators to float32 API arrays:
+ * reaction [tools][3], torque [tools][3], board [3], work [1]. */
+int bm_read_accumulators(bm_solver* s, float* reaction, float* torque, float* board, float* work, void* stream);
+/* Overwrite the accumulators from float32 API arrays (any may be NULL). */
+int bm_write_accumulators(bm_solver* s, const float* reaction, const float* torque, const float* board,
+                          const float* work, void* stream);
+/* Write the tool float32 mirror from the float64 tool state (after host writes). */
+int bm_sync_tool_mirror(bm_solver* s, void* stream);
+
+/* Kernel-level entry points on caller buffers, used by unit tests and by
+ * callers of the reference's @wp.func helpers. */
+/* contact.blade_query (contact.py:46-120), n points (AoS float3). */
+int bm_blade_query(const float* local, int n, const float* half, float bevel, float* closest, float* normal,
+                   float* distance, void* stream);
+/* contact.friction (contact.py:21-43), normal/relative/history AoS float3 [n]. */
+int bm_friction(const float* normal, const float* relative, const float* jn, const float* history, int n, float me,
+                float dt, float mus, float mud, float gk, float gc, float* impulse, float* new_history, void* stream);
+/* material.couple over explicit node lists (material.py:155-193): fields are
+ * given per node as runs in `order` (ascending code), AoS float3 state. */
+int bm_couple_fields(const int64_t* codes, const float* mass, const float* state, const int32_t* node_start,
+                     int nodes, float* result, void* stream);
+/* material.g2p (material.py:343-381) on explicit slots/weights (AoS float3). */
+int bm_g2p_probe(float* x, float* v, const int32_t* slots, const float* weights, const float* old_v,
+                 const float* new_v, int n, float dt, float flip, void* stream);
+/* contact.resist_cut (contact.py:181-232) for n particles (AoS float3 inputs). */
+int bm_resist_cut_probe(const float* j, const float* x, const float* v, const float* origin,
+                        const float* tool_velocity, const float* q, const float* tool_angular, const float* half,
+                        float radius, float spacing, float* damage, float threshold, int cutting, uint64_t* work_acc,
+                        float* result, int n, void* stream);
+/* material.plastic_project (material.py:434-442) on [9][n] F and Fp. */
+int bm_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLADEMASTER_GB300_H */

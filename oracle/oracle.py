@@ -1,0 +1,398 @@
+"""CPU ORACLE wrapper - test infrastructure, not part of the product.
+
+Loads oracle/oracle.c (built here with gcc -ffp-contract=off -fopenmp) and
+drives it like the reference's Solver (blademaster_warp/solver.py), so tests
+can run the same scene on the GPU product and on this restatement and
+compare.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg use it.
+
+Setup shared with the product: particle sampling and stencils come from
+``blademaster_gb300.geometry`` (pinned bit-exactly against the reference's
+geometry.points / stencil by tests/test_geometry.py), and the parameter
+struct layout from include/blademaster_gb300.h.  The solver constants
+(mass, Lame parameters, damage threshold, inertia, capacities) are derived
+here again from solver.py:164-200, independently of the product.
+"""
+
+import ctypes
+import os
+import subprocess
+import sys
+import threading
+from dataclasses import asdict
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "blademaster-lab_gb300"))
+
+from blademaster_gb300 import _native  # noqa: E402  (header-driven struct layout only)
+from blademaster_gb300.geometry import points, stencil, cell_sort  # noqa: E402
+
+HERE = Path(__file__).resolve().parent
+SOURCE = HERE / "oracle.c"
+LIBRARY = HERE / "_build" / "liboracle.so"
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle (portable flags: it runs on x86_64 and aarch64)."""
+    with _lock:
+        deps = [SOURCE, ROOT / "blademaster-lab_gb300" / "csrc" / "bm_scalar.h", ROOT / "include" / "blademaster_gb300.h"]
+        if not force and LIBRARY.exists() and all(d.stat().st_mtime <= LIBRARY.stat().st_mtime for d in deps):
+            return LIBRARY
+        LIBRARY.parent.mkdir(exist_ok=True)
+        tmp = LIBRARY.with_suffix(".tmp.so")
+        cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+               str(SOURCE), "-o", str(tmp), "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stderr)
+        os.replace(tmp, LIBRARY)
+        return LIBRARY
+
+
+P = ctypes.c_void_p
+_STATE_FIELDS = [
+    "x", "v", "ref", "F", "Fp", "stress", "viscous", "codes", "damage", "histories", "impulses", "nodes",
+    "weights", "gradients", "keys", "slots", "node_start", "node_slots", "slot_start", "contrib", "grid_mass",
+    "momentum", "grid_impulse", "old_v", "new_v", "remapped", "coupled", "pair_keys", "pair_history", "pair_used",
+    "pair_count", "cell_head", "cell_next", "tool", "mobility", "acc", "interval", "table_impulse", "speed",
+    "errors", "flags", "result",
+]
+
+
+class State(ctypes.Structure):
+    _fields_ = [(name, P) for name in _STATE_FIELDS] + [("capacity", ctypes.c_int64), ("buckets", ctypes.c_int64)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIBRARY))
+        if L.orc_state_size() != ctypes.sizeof(State):
+            raise RuntimeError("oracle state layout mismatch")
+        pp, ps, vp, i, f = ctypes.POINTER(_native.Params), ctypes.POINTER(State), ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        sig = {
+            "orc_register": [pp, ps, vp],
+            "orc_refresh_stress": [pp, ps],
+            "orc_plastic_project": [pp, ps, f],
+            "orc_material_step": [pp, ps, vp, i],
+            "orc_rigid_contacts": [pp, ps, i],
+            "orc_particle_contacts": [pp, ps],
+            "orc_assign": [pp, ps, i, i],
+            "orc_drive_one": [pp, ps, i, vp, vp],
+            "orc_accumulate_tool_impulses": [pp, ps],
+            "orc_finish_external": [pp, ps],
+            "orc_clear_step": [pp, ps],
+            "orc_load_external": [pp, ps, vp],
+            "orc_validate_interval": [pp, ps],
+            "orc_substep": [pp, ps, i, i, vp, i, vp, vp],
+            "orc_friction": [vp, vp, vp, vp, i, f, f, f, f, f, f, vp, vp],
+            "orc_blade_query": [vp, i, vp, f, vp, vp, vp],
+            "orc_resist_cut": [vp, vp, vp, vp, vp, vp, vp, vp, f, f, vp, f, i, vp, vp, i],
+        }
+        for name, args in sig.items():
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = None
+        L.orc_couple_fields.argtypes = [vp, vp, vp, vp, i, vp]
+        L.orc_g2p.argtypes = [vp, vp, vp, vp, vp, vp, i, f, f]
+        L.orc_math_f.argtypes = [vp, i, vp, vp]
+        L.orc_math_d.argtypes = [vp, vp, i, vp, vp, vp]
+        L.orc_svd.argtypes = [vp, i, vp, vp, vp, vp]
+        L.orc_fx_roundtrip.argtypes = [vp, i, vp]
+        for name in ("orc_couple_fields", "orc_g2p", "orc_math_f", "orc_math_d", "orc_svd", "orc_fx_roundtrip"):
+            getattr(L, name).restype = None
+        L.orc_count_embedded.argtypes = [pp, ps]
+        L.orc_count_embedded.restype = ctypes.c_int64
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def fx_to_float(lo, hi):
+    v = (int(np.uint64(hi)) << 64) | int(np.uint64(lo))
+    if v >= 1 << 127:
+        v -= 1 << 128
+    return v / 2.0**96
+
+
+def _pow2_at_least(v):
+    return 1 << (max(int(v), 1) - 1).bit_length()
+
+
+class OracleSolver:
+    """The reference's Solver restated on the CPU (device particle order, AoS arrays)."""
+
+    def __init__(self, config):
+        cfg = self.config = config
+        self.L = lib()
+        self.reference, self.origin, cells = points(cfg.size, cfg.grid_spacing, cfg.shape, cfg.sampling_seed)
+        n = self.n = len(self.reference)
+        nodes, w, g = stencil(self.reference, self.origin, cfg.grid_spacing, cells)
+        order, _ = cell_sort(self.reference, self.origin, cfg.grid_spacing, cells)
+        self.order = order
+        self.rank = np.empty(n, np.int64)
+        self.rank[order] = np.arange(n)
+        self.node_count = int(np.prod(cells + 1))
+        self.node_numpy, self.weight_numpy = nodes, w
+        # solver.py:181-200
+        volume = (cfg.grid_spacing / 2) ** 3
+        mass = cfg.density * volume
+        radius = cfg.grid_spacing / 4
+        blade_offset = max(cfg.blade_contact_radius or radius, radius - cfg.blade_half_size[0])
+        mu = cfg.young_modulus / (2 * (1 + cfg.poisson_ratio))
+        lam = cfg.young_modulus * cfg.poisson_ratio / ((1 + cfg.poisson_ratio) * (1 - 2 * cfg.poisson_ratio))
+        maxwell = cfg.maxwell_tau > 0 and cfg.maxwell_fraction > 0
+        threshold = cfg.cutting_energy * volume ** (2 / 3) * (1 - cfg.sharpness) / cfg.sharpness
+        ratio = 1.0 if cfg.contact_reference_dt == 0 else (cfg.dt / cfg.contact_reference_dt) ** 2
+        sn, gk = cfg.normal_scale * ratio, cfg.tangent_stiffness * ratio
+        hx, hy, hz = cfg.blade_half_size
+        inertia_inv = 3 / (cfg.blade_mass * np.array([hy * hy + hz * hz, hx * hx + hz * hz, hx * hx + hy * hy]))
+        self.mass, self.volume, self.radius, self.mu, self.lam = mass, volume, radius, mu, lam
+        K = cfg.tool_count
+        pair_list = cfg.pair_search in ("list", "auto")
+        p = _native.Params()
+        p.n, p.node_count, p.tool_count = n, self.node_count, K
+        p.pair_capacity = _pow2_at_least(max(64 * n, 16))
+        p.tool_model = -1 if cfg.external_tool else int(cfg.free_blade or cfg.pose_servo)
+        p.external_tool = int(cfg.external_tool)
+        p.predict = int(cfg.tool_substep == "predict")
+        p.free_blade = int(cfg.free_blade)
+        p.lock_rotation = int(not (cfg.free_blade or cfg.pose_servo))
+        p.accumulate_tool_impulses = int(cfg.accumulate_tool_impulses)
+        p.plastic = int(cfg.yield_stress > 0)
+        p.use_fp = int(cfg.yield_stress > 0 or maxwell)
+        p.maxwell = int(maxwell)
+        p.viscous = int(cfg.dynamic_viscosity > 0)
+        p.pair_search = 0 if pair_list else 1
+        p.cache_topology = int(cfg.cache_topology)
+        p.dt, p.spacing, p.mass, p.volume, p.radius, p.mu, p.lam = cfg.dt, cfg.grid_spacing, mass, volume, radius, mu, lam
+        p.mu_maxwell = cfg.maxwell_fraction * mu
+        p.maxwell_relax = float(-np.expm1(-cfg.dt / cfg.maxwell_tau)) if maxwell else 0.0
+        p.yield_stress, p.flip, p.dynamic_viscosity = cfg.yield_stress, cfg.flip_fraction, cfg.dynamic_viscosity
+        p.normal_scale, p.tangent_stiffness = sn, gk
+        p.friction_static, p.friction_dynamic, p.tangent_damping = cfg.friction_static, cfg.friction_dynamic, cfg.tangent_damping
+        p.board_scale = cfg.board_normal_scale or sn
+        p.board_half[0], p.board_half[1] = cfg.board_half_extent
+        f32 = lambda v: float(np.float32(v))  # noqa: E731
+        for i in range(3):
+            p.half[i] = cfg.blade_half_size[i]
+            p.inertia_inv[i] = f32(inertia_inv[i])
+            p.half_d[i] = f32(cfg.blade_half_size[i])
+            p.inertia_inv_d[i] = f32(inertia_inv[i])
+        p.bevel, p.blade_offset, p.blade_mass, p.threshold = cfg.blade_bevel_height, blade_offset, cfg.blade_mass, threshold
+        p.pair_skin = (cfg.pair_skin or radius) if pair_list else 0.0
+        p.dt_d, p.blade_mass_d, p.bevel_d = f32(cfg.dt), f32(cfg.blade_mass), f32(cfg.blade_bevel_height)
+        p.drive_stiffness, p.drive_damping = f32(cfg.drive_stiffness), f32(cfg.drive_damping)
+        p.drive_force_limit = f32(cfg.drive_force_limit)
+        p.rot_stiffness, p.rot_damping = f32(cfg.rotational_stiffness), f32(cfg.rotational_damping)
+        p.friction_dynamic_d = f32(cfg.friction_dynamic)
+        p.board_half_d[0], p.board_half_d[1] = f32(cfg.board_half_extent[0]), f32(cfg.board_half_extent[1])
+        self.params = p
+        cap = _pow2_at_least(max(16 * n, 16))
+        A = self.arrays = {}
+        A["x"] = np.ascontiguousarray(self.reference[order], np.float32)
+        A["v"] = np.zeros((n, 3), np.float32)
+        A["ref"] = A["x"].copy()
+        A["F"] = np.tile(np.eye(3, dtype=np.float32).reshape(9), (n, 1))
+        A["Fp"] = A["F"].copy()
+        A["stress"] = np.zeros((n, 9), np.float32)
+        A["viscous"] = np.zeros((n, 9), np.float64)
+        A["codes"] = np.zeros(n, np.int64)
+        A["zero_codes"] = np.zeros(n, np.int64)
+        A["damage"] = np.zeros((K, n), np.float32)
+        A["histories"] = np.zeros((1 + K, n, 3), np.float32)
+        A["impulses"] = np.zeros((n, 3), np.float32)
+        A["nodes"] = np.ascontiguousarray(nodes[order], np.int32)
+        A["weights"] = np.ascontiguousarray(w[order], np.float32)
+        A["gradients"] = np.ascontiguousarray(g[order], np.float32)
+        A["keys"] = np.full(cap, -1, np.int64)
+        A["slots"] = np.zeros((n, 8), np.int32)
+        A["node_start"] = np.zeros(self.node_count + 1, np.int32)
+        A["node_slots"] = np.zeros(cap, np.int32)
+        A["slot_start"] = np.zeros(cap + 1, np.int32)
+        A["contrib"] = np.zeros(8 * n, np.int32)
+        A["grid_mass"] = np.zeros(cap, np.float32)
+        for k in ("momentum", "grid_impulse", "old_v", "new_v", "remapped", "coupled"):
+            A[k] = np.zeros((cap, 3), np.float32)
+        A["pair_keys"] = np.full((2, p.pair_capacity), -1, np.int64)
+        A["pair_history"] = np.zeros((2, p.pair_capacity, 3), np.float32)
+        A["pair_used"] = np.zeros((2, p.pair_capacity), np.int32)
+        A["pair_count"] = np.zeros(2, np.int32)
+        buckets = _pow2_at_least(max(2 * n, 1024))
+        A["cell_head"] = np.zeros(buckets, np.int32)
+        A["cell_next"] = np.zeros(n, np.int32)
+        tool = np.zeros((K, 13))
+        tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
+        tool[:, 9] = 1.0
+        A["tool"] = tool
+        A["mobility"] = np.zeros(36, np.float32)
+        A["acc"] = np.zeros(_native.ACC_WORDS, np.uint64)
+        A["interval"] = np.zeros(6)
+        A["table_impulse"] = np.zeros((K, 3))
+        A["speed"] = np.zeros(1, np.float32)
+        A["errors"] = np.zeros(3, np.int32)
+        A["flags"] = np.zeros(_native.FLAG["WORDS"], np.int32)
+        A["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
+        A["result"] = np.zeros(10 + 7 * 4097, np.float32)
+        s = State()
+        for name in _STATE_FIELDS:
+            setattr(s, name, A[name].ctypes.data)
+        s.capacity, s.buckets = cap, buckets
+        self.S = s
+        self.single_field = False
+        self.step_count = 0
+        self.cut_index = 0
+        self.refresh_stress()
+
+    # ------------------------------------------------------------- access
+
+    def get(self, name):
+        """Array in reference particle order (particle arrays) or as stored."""
+        A = self.arrays
+        if name in ("x", "v", "ref", "impulses"):
+            return A[name][self.rank]
+        if name in ("F", "Fp", "stress"):
+            return A[name][self.rank].reshape(-1, 3, 3)
+        if name in ("codes", "damage"):
+            return A[name][self.rank] if name == "codes" else A["damage"][0][self.rank]
+        if name == "tool_damage":
+            return A["damage"][:, self.rank]
+        if name == "histories":
+            return A["histories"][:2][:, self.rank]
+        if name in ("reaction", "torque"):
+            base = 0 if name == "reaction" else 2 * 3 * _native.MAX_TOOLS
+            acc = A["acc"]
+            return np.array(
+                [[fx_to_float(acc[base + 6 * k + 2 * i], acc[base + 6 * k + 2 * i + 1]) for i in range(3)]
+                 for k in range(self.config.tool_count)]
+            )
+        if name == "board":
+            acc = A["acc"]
+            b = 2 * 6 * _native.MAX_TOOLS
+            return np.array([[fx_to_float(acc[b + 2 * i], acc[b + 2 * i + 1]) for i in range(3)]])
+        if name == "work":
+            acc = A["acc"]
+            b = 2 * (6 * _native.MAX_TOOLS + 3)
+            return np.array([fx_to_float(acc[b], acc[b + 1])])
+        if name == "tool_pos":
+            return A["tool"][:, 0:3]
+        if name == "tool_vel":
+            return A["tool"][:, 3:6]
+        if name == "tool_rot":
+            return A["tool"][:, 6:10]
+        if name == "tool_omega":
+            return A["tool"][:, 10:13]
+        return A[name]
+
+    def set(self, name, value):
+        """Write an array given in reference particle order (particle arrays) or as stored."""
+        A = self.arrays
+        value = np.asarray(value)
+        if name in ("x", "v", "ref", "impulses"):
+            A[name][:] = value.reshape(-1, 3)[self.order]
+        elif name in ("F", "Fp"):
+            A[name][:] = value.reshape(-1, 9)[self.order]
+            if name == "Fp" and not np.all(A["Fp"] == np.eye(3, dtype=np.float32).reshape(9)):
+                self.params.use_fp = 1
+        elif name == "codes":
+            A["codes"][:] = value[self.order]
+            A["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
+        elif name == "damage":
+            A["damage"][0][:] = value[self.order]
+        elif name == "tool_pos":
+            A["tool"][:, 0:3] = np.asarray(value, np.float32).reshape(-1, 3)
+        elif name == "tool_vel":
+            A["tool"][:, 3:6] = np.asarray(value, np.float32).reshape(-1, 3)
+        elif name == "tool_rot":
+            A["tool"][:, 6:10] = np.asarray(value, np.float32).reshape(-1, 4)
+        elif name == "tool_omega":
+            A["tool"][:, 10:13] = np.asarray(value, np.float32).reshape(-1, 3)
+        elif name == "mobility":
+            A["mobility"][:] = np.asarray(value, np.float32).reshape(36)
+        else:
+            A[name][...] = value
+
+    # ------------------------------------------------------------- physics
+
+    def _field_codes(self):
+        return ptr(self.arrays["zero_codes"] if self.single_field else self.arrays["codes"])
+
+    def refresh_stress(self):
+        self.L.orc_refresh_stress(ctypes.byref(self.params), ctypes.byref(self.S))
+
+    def material_step(self):
+        force = (not self.config.cache_topology) or self.arrays["flags"][_native.FLAG["TOPOLOGY_DIRTY"]]
+        self.L.orc_material_step(ctypes.byref(self.params), ctypes.byref(self.S), self._field_codes(), int(bool(force)))
+
+    def register(self):
+        self.L.orc_register(ctypes.byref(self.params), ctypes.byref(self.S), self._field_codes())
+
+    def rigid_contacts(self, cut_bits=1):
+        self.L.orc_rigid_contacts(ctypes.byref(self.params), ctypes.byref(self.S), int(cut_bits))
+
+    def particle_contacts(self):
+        self.arrays["flags"][_native.FLAG["STEP"]] = self.step_count
+        self.L.orc_particle_contacts(ctypes.byref(self.params), ctypes.byref(self.S))
+
+    def assign_sides(self, cut_index, cutting=True):
+        self.L.orc_assign(ctypes.byref(self.params), ctypes.byref(self.S), int(cut_index), int(bool(cutting)))
+
+    def cut_bits(self, cutting):
+        if not cutting:
+            return 0
+        cfg = self.config
+        return 1 | (2 if cfg.cut_work == "advance" else 0) | (4 if cfg.cut_hold else 0)
+
+    def set_cut(self, cut_index):
+        if cut_index != self.cut_index:
+            self.arrays["damage"][:] = 0
+            self.cut_index = cut_index
+
+    def step(self, target_edge=(0.0, 0.0, 0.042), cutting=True, cut_index=0, orientation=None):
+        self.set_cut(cut_index)
+        self.arrays["flags"][_native.FLAG["STEP"]] = self.step_count
+        target = np.asarray(target_edge, np.float32).reshape(3)
+        rot = np.asarray(orientation if orientation is not None else [0, 0, 0, 1], np.float32).reshape(4)
+        self.L.orc_substep(ctypes.byref(self.params), ctypes.byref(self.S), self.cut_bits(cutting), int(cut_index),
+                           self._field_codes(), int(self.config.cache_topology), ptr(target), ptr(rot))
+        self.step_count += 1
+
+    def advance(self, targets, cutting=True, cut_index=0, orientations=None):
+        targets = np.asarray(targets, np.float32)
+        if orientations is None:
+            orientations = np.tile([0, 0, 0, 1.0], (len(targets), 1))
+        orientations = np.asarray(orientations, np.float64)
+        orientations = (orientations / np.linalg.norm(orientations, axis=1)[:, None]).astype(np.float32)
+        for t, q in zip(targets, orientations):
+            self.step(t, cutting, cut_index, q)
+
+    def external_interval(self, state_packed, steps, cutting=True, cut_index=0):
+        """ExternalToolPort.advance (coupling.py:88-189): returns (impulse, angular about the world origin, errors)."""
+        self.set_cut(cut_index)
+        packed = np.asarray(state_packed, np.float32)
+        self.L.orc_load_external(ctypes.byref(self.params), ctypes.byref(self.S), ptr(packed))
+        dummy_t = np.zeros(3, np.float32)
+        dummy_q = np.array([0, 0, 0, 1], np.float32)
+        for _ in range(steps):
+            self.arrays["flags"][_native.FLAG["STEP"]] = self.step_count
+            self.L.orc_substep(ctypes.byref(self.params), ctypes.byref(self.S), self.cut_bits(cutting), int(cut_index),
+                               self._field_codes(), int(self.config.cache_topology), ptr(dummy_t), ptr(dummy_q))
+            self.step_count += 1
+        self.L.orc_validate_interval(ctypes.byref(self.params), ctypes.byref(self.S))
+        return self.arrays["interval"][:3].copy(), self.arrays["interval"][3:].copy(), self.arrays["errors"].copy()
+
+    def num_threads(self):
+        return self.L.orc_num_threads()
+
+
+def config_dict(cfg):
+    return asdict(cfg)

@@ -1,0 +1,145 @@
+"""CUDA path against the CPU oracle on the same inputs.
+
+Bit-exact (assert_array_equal) for everything the kernels compute: particle
+state, stress, cut codes, damage, (node, code) fields, contact reactions.
+Both sides evaluate the same operation sequence (no fused multiply-add, the
+same elementary functions, every reduction in ascending particle order), so
+any difference is a bug, not rounding.
+"""
+
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+from blademaster_gb300.solver import Config, Solver
+from blademaster_gb300.coupling import ExternalToolPort, ToolState
+from oracle.oracle import OracleSolver
+
+pytestmark = pytest.mark.gpu
+
+EXACT = ("x", "v", "F", "stress", "codes", "damage")
+
+
+def both(cfg):
+    return Solver(cfg), OracleSolver(cfg)
+
+
+def assert_same(gpu, cpu, names=EXACT):
+    for name in names:
+        np.testing.assert_array_equal(getattr(gpu, name).numpy(), cpu.get(name), err_msg=name)
+    assert gpu.errors.numpy().tolist() == cpu.get("errors").tolist()
+
+
+def key_map(solver_like, slots, keys):
+    """particle -> (node, code) key of each stencil node."""
+    return keys[slots]
+
+
+@pytest.mark.parametrize("viscosity", [0.0, 2.0])
+def test_material_step_with_random_fields_is_bitexact(viscosity):
+    # the fixture of tests/test_compact_grid.py:14-22
+    cfg = Config(dynamic_viscosity=viscosity)
+    g, c = both(cfg)
+    rng = np.random.default_rng(23)
+    velocity = rng.normal(0, 0.01, (g.n, 3))
+    codes = rng.integers(0, 27, g.n).astype(np.int64)
+    impulse = rng.normal(0, 1.0e-7, (g.n, 3))
+    for s in (g, c):
+        if isinstance(s, Solver):
+            s.v.assign(velocity)
+            s.codes.assign(codes)
+            s.impulses.assign(impulse)
+        else:
+            s.set("v", velocity.astype(np.float32))
+            s.set("codes", codes)
+            s.set("impulses", impulse.astype(np.float32))
+    g.material_step()
+    c.material_step()
+    assert_same(g, c, ("x", "v", "F", "stress"))
+    # (node, code) key set and the particle -> key map (test_compact_grid.py:25-26)
+    gk = g.keys.numpy()
+    np.testing.assert_array_equal(np.sort(gk[gk >= 0]), np.sort(c.get("keys")[c.get("keys") >= 0]))
+    gmap = gk[g.slots.numpy()]
+    cmap = c.get("keys")[c.get("slots")][c.rank]
+    np.testing.assert_array_equal(gmap, cmap)
+    np.testing.assert_allclose(g.mass * g.v.numpy().astype(float).sum(0),
+                               g.mass * (velocity.astype(np.float32).astype(float).sum(0)) + impulse.astype(np.float32).astype(float).sum(0), atol=2e-9)
+
+
+@pytest.mark.parametrize("yield_stress", [0.0, 2000.0])
+def test_guided_cut_substeps_are_bitexact(yield_stress):
+    cfg = replace(Config(), yield_stress=yield_stress)
+    g, c = both(cfg)
+    g.tool_pos.assign([[0.0, 0.0, 0.047]])
+    c.set("tool_pos", [[0.0, 0.0, 0.047]])
+    for i in range(60):
+        g.step((0.0, 0.0, 0.02), cutting=True)
+        c.step((0.0, 0.0, 0.02), cutting=True)
+    assert_same(g, c, EXACT + ("Fp",))
+    np.testing.assert_array_equal(g.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
+    np.testing.assert_array_equal(g.reaction.numpy(), c.get("reaction").astype(np.float32))
+    np.testing.assert_array_equal(g.work.numpy(), c.get("work").astype(np.float32))
+    assert np.count_nonzero(g.codes.numpy()) > 0
+
+
+def test_graph_replay_is_bitexact_with_eager_and_oracle():
+    cfg = replace(Config(), free_blade=True)
+    eager, graphed = Solver(cfg), Solver(cfg)
+    c = OracleSolver(cfg)
+    for s in (eager, graphed):
+        s.tool_pos.assign([[0.0, 0.0, 0.047]])
+    c.set("tool_pos", [[0.0, 0.0, 0.047]])
+    for n, cut, on in [(5, 0, True), (6, 0, True), (5, 0, False), (6, 1, True)]:
+        targets = np.zeros((n, 3))
+        eager.advance(targets, on, cut, graph=False)
+        graphed.advance(targets, on, cut, graph=True)
+        c.advance(targets, on, cut)
+        for name in EXACT:
+            np.testing.assert_array_equal(eager.__getattribute__(name).numpy(), graphed.__getattribute__(name).numpy(), err_msg=name)
+        assert_same(graphed, c)
+        np.testing.assert_array_equal(graphed.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
+
+
+def test_external_interval_matches_oracle():
+    cfg = replace(Config(), external_tool=True)
+    g, c = both(cfg)
+    x = g.x.numpy()
+    x[:, 2] += 0.1
+    g.x.assign(x)
+    c.set("x", x)
+    angle = 0.15
+    state = ToolState([0.001, 0.0, 0.132], [0.0, np.sin(angle / 2), 0.0, np.cos(angle / 2)], [0.01, 0.0, -0.02], [0.0, 0.1, 0.0])
+    port = ExternalToolPort(g)
+    checked = state.checked()
+    packed = np.concatenate([checked.position, checked.orientation_xyzw, checked.linear_velocity,
+                             checked.angular_velocity, checked.mobility.ravel()]).astype(np.float32)
+    for _ in range(3):
+        r = port.advance(state, 8 * cfg.dt, cutting=False)
+        imp, ang, err = c.external_interval(packed, 8, cutting=False)
+        np.testing.assert_array_equal(r.impulse_ns, imp)
+        assert not err.any()
+    assert_same(g, c)
+
+
+def test_pair_contact_impulses_are_equal_and_opposite():
+    # tests/test_pair_list.py:11-46 scene: two particles on opposite sides, closing
+    cfg = Config(size=(0.018, 0.018, 0.018), grid_spacing=0.006, dt=0.001, grid_storage="compact")
+    for mode in ("list", "hash"):
+        g, c = both(replace(cfg, pair_search=mode))
+        x = np.zeros((g.n, 3), np.float32)
+        x[:, 0] = np.arange(g.n) * 0.1 + 2
+        x[:, 2] = 0.1
+        x[:2] = [[0, 0, 0.1], [0.0048, 0, 0.1]]
+        v = np.zeros_like(x)
+        v[:2] = [[1.0, 0, 0], [-1.0, 0, 0]]
+        codes = np.zeros(g.n, np.int64)
+        codes[:2] = [1, 2]
+        g.x.assign(x), g.v.assign(v), g.codes.assign(codes), g.speed.fill_(1.0)
+        c.set("x", x), c.set("v", v), c.set("codes", codes), c.set("speed", np.array([1.0], np.float32))
+        g.particle_contacts()
+        c.particle_contacts()
+        gi = g.impulses.numpy()
+        np.testing.assert_array_equal(gi, c.get("impulses"))
+        assert g.pair_count[1].numpy()[0] == 1
+        assert np.all(gi[0] == -gi[1]) and np.any(gi[0] != 0)
