@@ -132,6 +132,7 @@ PAIR_LANES = int(header_constant("BM_PAIR_LANES"))
 MAX_TOOLS = int(header_constant("BM_MAX_TOOLS"))
 FLAG = {k: int(header_constant("BM_FLAG_" + k)) for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "WORDS")}
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
+STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate"]
 ACC_WORDS = 2 * (6 * MAX_TOOLS + 4)
 
 
@@ -158,6 +159,7 @@ def _declare(lib):
         "bm_clear_step": ([vp, vp], i),
         "bm_substeps": ([vp, ctypes.POINTER(StepArgs), vp], i),
         "bm_graph_create": ([vp, ctypes.POINTER(StepArgs), vp, ctypes.POINTER(vp)], i),
+        "bm_substeps_profiled": ([vp, ctypes.POINTER(StepArgs), vp, vp], i),
         "bm_graph_launch": ([vp, vp], i),
         "bm_graph_destroy": ([vp], i),
         "bm_count_embedded": ([vp, i, vp], i),

@@ -42,25 +42,55 @@ void layout_scratch(bm_solver* s) {
     s->viscous_scratch = reinterpret_cast<float*>(base + off);
 }
 
+// Optional CUDA events around each stage of a substep (profiling only).
+struct StageTimer {
+    cudaEvent_t ev[BM_STAGES + 1];
+    bool on = false;
+    void mark(int i, cudaStream_t st) {
+        if (on) cudaEventRecord(ev[i], st);
+    }
+};
+
 // One batch of substeps on stream st.
-int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st) {
+int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* timer = nullptr,
+              float* stage_ms = nullptr) {
     const bm_params& P = s->P;
     const int64_t* field_codes = a->single_field ? s->B.zero_codes : s->B.codes;
+    StageTimer none;
+    StageTimer& t = timer ? *timer : none;
     if (a->external_load) bm::launch_load_external(s, st);
     if (a->record_samples) bm::launch_record_pose(s, 0, st);
     for (int i = 0; i < a->steps; ++i) {
+        t.mark(0, st);
         bm::launch_prologue(s, P.external_tool ? 0 : 1, st);
+        t.mark(1, st);
         bm::launch_rigid(s, a->cut_bits, st);
+        t.mark(2, st);
         bm::launch_pairs(s, st);
+        t.mark(3, st);
         bm::launch_register(s, field_codes, P.cache_topology ? 0 : 1, st);
+        t.mark(4, st);
         bm::launch_material(s, 0, st);
+        t.mark(5, st);
         bm::launch_g2p(s, st);
+        t.mark(6, st);
         bm::launch_remap(s, st);
+        t.mark(7, st);
         int mode = bm::kToolDrive;
         if (P.external_tool) mode = bm::kToolFinishExternal;
         else if (P.accumulate_tool_impulses) mode = bm::kToolAccumulate;
         bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
+        t.mark(8, st);
         bm::launch_fupdate_assign(s, 1, a->cut_index, a->cut_bits != 0, st);
+        t.mark(9, st);
+        if (t.on) {
+            if (cudaEventSynchronize(t.ev[BM_STAGES]) != cudaSuccess) return check_cuda("profiled substep");
+            for (int k = 0; k < BM_STAGES; ++k) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, t.ev[k], t.ev[k + 1]);
+                stage_ms[k] += ms;
+            }
+        }
         if (a->record_samples && (!a->hold_pose || i == a->steps - 1))
             bm::launch_record_pose(s, a->hold_pose ? 1 : i + 1, st);
     }
@@ -208,6 +238,17 @@ int bm_substeps(bm_solver* s, const bm_step_args* args, void* stream) {
     if (!s || !args) return fail(BM_ERR_ARGUMENT, "null argument");
     if (args->steps < 0) return fail(BM_ERR_ARGUMENT, "steps must be non-negative");
     return run_batch(s, args, as_stream(stream));
+}
+
+int bm_substeps_profiled(bm_solver* s, const bm_step_args* args, float* stage_ms, void* stream) {
+    if (!s || !args || !stage_ms) return fail(BM_ERR_ARGUMENT, "null argument");
+    StageTimer timer;
+    for (int k = 0; k <= BM_STAGES; ++k) cudaEventCreate(&timer.ev[k]);
+    for (int k = 0; k < BM_STAGES; ++k) stage_ms[k] = 0.0f;
+    timer.on = true;
+    int rc = run_batch(s, args, as_stream(stream), &timer, stage_ms);
+    for (int k = 0; k <= BM_STAGES; ++k) cudaEventDestroy(timer.ev[k]);
+    return rc;
 }
 
 int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_graph** out) {

@@ -228,6 +228,24 @@ int bm_substeps(bm_solver* s, const bm_step_args* args, void* stream);
 int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_graph** out);
 int bm_graph_launch(bm_graph* g, void* stream);
 int bm_graph_destroy(bm_graph* g);
+/* Stages of one substep, in launch order (profiling). */
+#define BM_STAGE_PROLOGUE 0  /* clear_pair_slots + clear_step */
+#define BM_STAGE_RIGID 1     /* rigid_and_speed + extra_blade */
+#define BM_STAGE_PAIRS 2     /* pair list rebuild (when needed) + pairs_listed */
+#define BM_STAGE_REGISTER 3  /* _register_topology (when needed) */
+#define BM_STAGE_P2G 4       /* p2g + couple_and_velocity */
+#define BM_STAGE_G2P 5       /* g2p of g2p_remap */
+#define BM_STAGE_REMAP 6     /* remap scatter + couple */
+#define BM_STAGE_TOOL 7      /* tool.step / finish_external_step */
+#define BM_STAGE_FUPDATE 8   /* update_F + stress + assign */
+#define BM_STAGES 9
+
+/* The batch of bm_substeps launched eagerly with a CUDA event pair around
+ * every stage; stage_ms[BM_STAGES] receives the summed device time of each
+ * stage over the batch (the host waits after every substep).  Results are
+ * identical to bm_substeps. */
+int bm_substeps_profiled(bm_solver* s, const bm_step_args* args, float* stage_ms, void* stream);
+
 /* contact.count_embedded (contact.py:1042-1055) into flags[BM_FLAG_EMBEDDED]. */
 int bm_count_embedded(bm_solver* s, int reset, void* stream);
 /* material.validate_interval (material.py:6-20). */

@@ -889,21 +889,27 @@ static int pair_impulse(const bm_params* P, orc_state* S, int64_t p, int64_t q, 
     oslot = find_key(S->pair_keys + (int64_t)old * P->pair_capacity, key, P->pair_capacity);
     if (oslot >= 0) history = ld3(S->pair_history + 3 * (int64_t)old * P->pair_capacity, oslot);
     if (!owner) history = v3_neg(history);
-    if (owner) {
-        nslot = insert_key(S->pair_keys + (int64_t)nw * P->pair_capacity, key, P->pair_capacity);
-        if (nslot < 0) {
-            *err0 += 1;
-            return 0;
-        }
-    }
     half_mass = P->mass / 2.0f;
     jn = P->normal_scale * half_mass / P->dt * predicted;
     friction(normal, relative, jn, history, half_mass, P->dt, P->friction_static, P->friction_dynamic,
              P->tangent_stiffness, P->tangent_damping, &jt, &ht);
     if (owner) {
-        st3(S->pair_history + 3 * (int64_t)nw * P->pair_capacity, nslot, ht);
-        S->pair_used[(int64_t)nw * P->pair_capacity + S->pair_count[nw]] = (int32_t)nslot;
-        S->pair_count[nw] += 1;
+        int failed = 0;
+#pragma omp critical(orc_pair_table)
+        {
+            nslot = insert_key(S->pair_keys + (int64_t)nw * P->pair_capacity, key, P->pair_capacity);
+            if (nslot < 0) {
+                failed = 1;
+            } else {
+                st3(S->pair_history + 3 * (int64_t)nw * P->pair_capacity, nslot, ht);
+                S->pair_used[(int64_t)nw * P->pair_capacity + S->pair_count[nw]] = (int32_t)nslot;
+                S->pair_count[nw] += 1;
+            }
+        }
+        if (failed) {
+            *err0 += 1;
+            return 0;
+        }
     }
     *out = v3_add(v3_mul(normal, jn), jt);
     return 1;
@@ -930,7 +936,6 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
     float reach = 2.0f * P->radius + 2.0f * P->dt * S->speed[0];
     int64_t mask = S->buckets - 1;
     int32_t err0 = 0, err2 = 0;
-    int64_t* list = (int64_t*)malloc(sizeof(int64_t) * 4096);
     for (i = 0; i < S->pair_count[nw]; ++i)
         S->pair_keys[(int64_t)nw * P->pair_capacity + S->pair_used[(int64_t)nw * P->pair_capacity + i]] = -1;
     S->pair_count[nw] = 0;
@@ -941,6 +946,10 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
         S->cell_next[p] = S->cell_head[b];
         S->cell_head[b] = (int32_t)p;
     }
+#pragma omp parallel
+    {
+    int64_t* list = (int64_t*)malloc(sizeof(int64_t) * 4096);
+#pragma omp for schedule(dynamic, 1024) reduction(+ : err0, err2)
     for (p = 0; p < n; ++p) {
         bm_v3 xp = ld3(S->x, p), total = ld3(S->impulses, p);
         int64_t cx = cell_coord(xp.x, reach), cy = cell_coord(xp.y, reach), cz = cell_coord(xp.z, reach), count = 0;
@@ -957,9 +966,9 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
             }
         }
         qsort(list, (size_t)count, sizeof(int64_t), cmp_i64);
-        for (i = 0; i < count; ++i) {
+        for (int64_t li = 0; li < count; ++li) {
             bm_v3 j;
-            if (pair_impulse(P, S, p, list[i], old, nw, &j, &err0, &err2)) {
+            if (pair_impulse(P, S, p, list[li], old, nw, &j, &err0, &err2)) {
                 total = v3_add(total, j);
                 touched = 1;
             }
@@ -967,6 +976,7 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
         if (touched) st3(S->impulses, p, total);
     }
     free(list);
+    }
     S->errors[0] += err0;
     S->errors[2] += err2;
 }
@@ -981,6 +991,7 @@ ORC_API void orc_assign(const bm_params* P, orc_state* S, int cut_index, int cut
         int e;
         for (e = 0; e < cut_index + k; ++e) digit *= 3;
         if (cutting == 0) continue;
+#pragma omp parallel for schedule(static) reduction(| : dirty)
         for (p = 0; p < P->n; ++p) {
             bm_v3 xp = ld3(S->x, p), edge, local, edge_v, d, edge_here;
             float front, advance, back;
