@@ -251,6 +251,9 @@ class Solver:
         T["grid_mass"] = zeros(S)
         for name in ("momentum", "grid_impulse", "old_v", "new_v", "remapped", "remap_v"):
             T[name] = zeros(3, S)
+        T["cell_part"] = zeros(7, 8, self.node_count)
+        T["cell_field"] = zeros(8, self.node_count, dtype=t.uint8)
+        T["hist_mask"] = t.full((n,), -1, dtype=t.int16, device=dev)
         T["built_x"] = zeros(3, n)
         T["built_codes"] = zeros(n, dtype=i64)
         T["partners"] = zeros(n, PAIR_LIST_LANES, dtype=i32)
@@ -268,7 +271,7 @@ class Solver:
         tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
         tool[:, 9] = 1.0
         T["tool"] = t.as_tensor(tool, device=dev)
-        T["tool_f"] = t.as_tensor(tool.astype(np.float32), device=dev)
+        T["tool_f"] = zeros(K, _native.TOOL_F_WORDS)
         T["mobility"] = zeros(36)
         T["acc"] = zeros(_native.ACC_WORDS, dtype=i64)
         T["interval"] = zeros(6, dtype=f64)
@@ -289,6 +292,7 @@ class Solver:
         T["flags"][_native.FLAG["PAIR_DIRTY"]] = 1
         self._handle = None
         self._bind()
+        self._call("bm_sync_tool_mirror", self._stream)
         self._views()
         self.field_codes = self.codes
         self.step_count = 0
@@ -444,9 +448,14 @@ class Solver:
         ]
         self.damage = self.tool_damage[0]
         self.impulses = particle_view(T["impulses"], o, r, (3,), np.float32, "impulses")
-        self.histories = particle_view(T["histories"][:2], o, r, (3,), np.float32, "histories", leading=2)
+        def histories_written():
+            T["hist_mask"].fill_(-1)
+
+        self.histories = particle_view(T["histories"][:2], o, r, (3,), np.float32, "histories", histories_written, leading=2)
         if K > 1:
-            self.extra_histories = particle_view(T["histories"][1:], o, r, (3,), np.float32, "extra_histories", leading=K)
+            self.extra_histories = particle_view(
+                T["histories"][1:], o, r, (3,), np.float32, "extra_histories", histories_written, leading=K
+            )
         else:
             self.extra_histories = None
         self.mobility_view = None

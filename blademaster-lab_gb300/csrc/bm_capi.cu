@@ -66,6 +66,20 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         t.mark(1, st);
         bm::launch_rigid(s, a->cut_bits, st);
         t.mark(2, st);
+        // The knife integration needs only this substep's reactions and is read
+        // only by the F update / side labels and the next substep, so (outside
+        // external mode, where the grid constraint may still change the
+        // reaction) it runs on a side stream concurrently with the transfers.
+        int mode = bm::kToolDrive;
+        if (P.external_tool) mode = bm::kToolFinishExternal;
+        else if (P.accumulate_tool_impulses) mode = bm::kToolAccumulate;
+        const bool fork = !t.on && !P.external_tool;
+        if (fork) {
+            cudaEventRecord(s->fork, st);
+            cudaStreamWaitEvent(s->side, s->fork, 0);
+            bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, s->side);
+            cudaEventRecord(s->join, s->side);
+        }
         bm::launch_pairs(s, st);
         t.mark(3, st);
         bm::launch_register(s, field_codes, P.cache_topology ? 0 : 1, st);
@@ -76,12 +90,10 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         t.mark(6, st);
         bm::launch_remap(s, st);
         t.mark(7, st);
-        int mode = bm::kToolDrive;
-        if (P.external_tool) mode = bm::kToolFinishExternal;
-        else if (P.accumulate_tool_impulses) mode = bm::kToolAccumulate;
-        bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
+        if (fork) cudaStreamWaitEvent(st, s->join, 0);
+        else bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
         t.mark(8, st);
-        bm::launch_fupdate_assign(s, 1, a->cut_index, a->cut_bits != 0, st);
+        bm::launch_fupdate_assign(s, 1, a->cut_index, a->cut_bits != 0, 1, st);
         t.mark(9, st);
         if (t.on) {
             if (cudaEventSynchronize(t.ev[BM_STAGES]) != cudaSuccess) return check_cuda("profiled substep");
@@ -146,7 +158,7 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
                               buffers->tool, buffers->tool_f, buffers->mobility, buffers->acc, buffers->interval,
                               buffers->table_impulse, buffers->speed, buffers->errors, buffers->flags,
                               buffers->targets, buffers->rotations, buffers->packed, buffers->result,
-                              buffers->scratch};
+                              buffers->scratch, buffers->cell_part, buffers->cell_field, buffers->hist_mask};
     for (const void* ptr : required)
         if (!ptr) return fail(BM_ERR_ARGUMENT, "a required buffer is null");
     if (P.maxwell && !buffers->viscous) return fail(BM_ERR_ARGUMENT, "maxwell requires the viscous buffer");
@@ -156,11 +168,22 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     s->B = *buffers;
     s->buckets = (int64_t)P.bucket_mask + 1;
     layout_scratch(s);
+    if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess) {
+        delete s;
+        return check_cuda("solver streams");
+    }
     *out = s;
     return BM_OK;
 }
 
 int bm_solver_destroy(bm_solver* s) {
+    if (!s) return BM_OK;
+    cudaStreamSynchronize(s->side);
+    cudaStreamDestroy(s->side);
+    cudaEventDestroy(s->fork);
+    cudaEventDestroy(s->join);
     delete s;
     return BM_OK;
 }
@@ -186,7 +209,7 @@ int bm_material_step(bm_solver* s, int single_field, void* stream) {
     bm::launch_material(s, 1, st);
     bm::launch_g2p(s, st);
     bm::launch_remap(s, st);
-    bm::launch_fupdate_assign(s, 1, 0, 0, st);
+    bm::launch_fupdate_assign(s, 1, 0, 0, 0, st);
     return check_cuda("material_step");
 }
 
@@ -206,7 +229,7 @@ int bm_particle_contacts(bm_solver* s, void* stream) {
 
 int bm_assign_sides(bm_solver* s, int cut_index, int cutting, void* stream) {
     if (!s) return fail(BM_ERR_ARGUMENT, "null solver");
-    bm::launch_fupdate_assign(s, 0, cut_index, cutting, as_stream(stream));
+    bm::launch_fupdate_assign(s, 0, cut_index, cutting, 0, as_stream(stream));
     return check_cuda("assign_sides");
 }
 

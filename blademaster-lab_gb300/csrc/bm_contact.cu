@@ -175,21 +175,38 @@ __device__ __forceinline__ bm_v3 resist_cut(bm_v3 j, bm_v3 xp, bm_v3 vp, bm_v3 o
 
 // contact.blade_at (contact.py:235-329) for knife k: returns the impulse on
 // the particle and sets the reaction / torque contributions (zero if none).
+// Two exact shortcuts keep far particles cheap without changing any result:
+// a particle outside the knife's box grown by the contact reach gets the
+// reference's "no contact" outcome directly, and bit 1 + k of `mask` says
+// whether its stored knife history may be non-zero (a zero history is
+// neither read nor rewritten).
 __device__ bm_v3 blade_at(const bm_params& P, const bm_buffers& B, int p, int k, const ToolF& T, int cutting,
-                          bm_v3* reaction, bm_v3* torque, bm_fx* work) {
+                          bm_v3 xp, bm_v3 vp, float vlen, float radius_of_blade, unsigned* mask, bm_v3* reaction,
+                          bm_v3* torque, bm_fx* work) {
     const int64_t N = P.n;
-    const bm_v3 xp = ld3(B.x, N, p), vp = ld3(B.v, N, p);
     float* hist = B.histories + (int64_t)(1 + k) * 3 * N;
-    float* damage = B.damage + (int64_t)k * N + p;
+    const unsigned bit = 1u << (1 + k);
     *reaction = v3_zero();
     *torque = v3_zero();
-    const float blade_radius = sqrtf((P.half[0] * P.half[0] + P.half[1] * P.half[1]) + P.half[2] * P.half[2]);
-    const float max_closing = v3_len(vp) + v3_len(T.vel) + v3_len(T.omega) * blade_radius;
-    if (v3_len(v3_sub(xp, T.pos)) - blade_radius - P.blade_offset > P.dt * max_closing) {
-        st3(hist, N, p, v3_zero());
+    const float max_closing = (vlen + T.speed) + T.spin_reach;
+    bool far = v3_len(v3_sub(xp, T.pos)) - radius_of_blade - P.blade_offset > P.dt * max_closing;
+    bm_v3 local = v3_zero();
+    if (!far) {
+        local = q_rotate_inv(T.rot, v3_sub(xp, T.pos));
+        // Contact needs every |local_i| <= half_i + offset + dt * max_closing;
+        // the margin is widened to cover rounding of the exact test below.
+        const float margin = (P.blade_offset + P.dt * max_closing) * 1.01f + 1.0e-6f;
+        far = fabsf(local.x) - P.half[0] > margin || fabsf(local.y) - P.half[1] > margin ||
+              fabsf(local.z) - P.half[2] > margin;
+    }
+    if (far) {
+        if (*mask & bit) {
+            st3(hist, N, p, v3_zero());
+            *mask &= ~bit;
+        }
         return v3_zero();
     }
-    const bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, T.pos));
+    float* damage = B.damage + (int64_t)k * N + p;
     bm_v3 closest_local, normal_local;
     float distance;
     blade_query(local, P.half, P.bevel, &closest_local, &normal_local, &distance);
@@ -204,14 +221,19 @@ __device__ bm_v3 blade_at(const bm_params& P, const bm_buffers& B, int p, int k,
     const bm_v3 n = q_rotate(T.rot, normal_local);
     const bm_v3 relative = v3_sub(v3_sub(vp, T.vel), v3_cross(T.omega, lever));
     if (distance - P.blade_offset + P.dt * bm_minf(v3_dot(relative, n), 0.0f) >= 0.0f) {
-        st3(hist, N, p, v3_zero());
+        if (*mask & bit) {
+            st3(hist, N, p, v3_zero());
+            *mask &= ~bit;
+        }
         return v3_zero();
     }
     const float me = blade_effective_mass(P, B.mobility, lever, n, T.rot);
+    const bm_v3 h_old = (*mask & bit) ? ld3(hist, N, p) : v3_zero();
     bm_v3 j, h;
-    penalty_impulse(distance - P.blade_offset, relative, n, me, ld3(hist, N, p), P.dt, P.normal_scale,
-                    P.friction_static, P.friction_dynamic, P.tangent_stiffness, P.tangent_damping, &j, &h);
+    penalty_impulse(distance - P.blade_offset, relative, n, me, h_old, P.dt, P.normal_scale, P.friction_static,
+                    P.friction_dynamic, P.tangent_stiffness, P.tangent_damping, &j, &h);
     st3(hist, N, p, h);
+    *mask |= bit;
     if (v3_len_sq(j) > 0.0f) {
         if (cutting != 0)
             j = resist_cut(j, xp, vp, T.pos, T.vel, T.rot, T.omega, P.half, P.blade_offset, P.spacing, damage,
@@ -237,19 +259,26 @@ __global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
     const int64_t N = P.n;
     bm_fx work = fx_zero();
     float speed = 0.0f;
-    bm_v3 total = v3_zero(), jb = v3_zero();
+    bm_v3 total = v3_zero(), jb = v3_zero(), xp = v3_zero(), vp = v3_zero();
     bool board_hit = false;
+    unsigned mask = 0u, mask_in = 0u;
+    const float radius_of_blade = blade_radius(P);
     if (active) {
-        const bm_v3 xp = ld3(B.x, N, p), vp = ld3(B.v, N, p);
+        xp = ld3(B.x, N, p);
+        vp = ld3(B.v, N, p);
+        mask = mask_in = B.hist_mask[p];
         speed = v3_len(vp);
         total = v3(0.0f, 0.0f, -9.81f * P.mass * P.dt);
         float board_gap = xp.z - P.radius;
         if (P.board_half[0] > 0.0f && fabsf(xp.x) > P.board_half[0]) board_gap = 1.0e30f;
         if (P.board_half[1] > 0.0f && fabsf(xp.y) > P.board_half[1]) board_gap = 1.0e30f;
         bm_v3 hb;
-        penalty_impulse(board_gap, vp, v3(0.0f, 0.0f, 1.0f), P.mass, ld3(B.histories, N, p), P.dt, P.board_scale,
-                        P.friction_static, P.friction_dynamic, P.tangent_stiffness, P.tangent_damping, &jb, &hb);
-        st3(B.histories, N, p, hb);
+        const bm_v3 h_old = (mask & 1u) ? ld3(B.histories, N, p) : v3_zero();
+        penalty_impulse(board_gap, vp, v3(0.0f, 0.0f, 1.0f), P.mass, h_old, P.dt, P.board_scale, P.friction_static,
+                        P.friction_dynamic, P.tangent_stiffness, P.tangent_damping, &jb, &hb);
+        const bool nonzero = hb.x != 0.0f || hb.y != 0.0f || hb.z != 0.0f;
+        if (nonzero || (mask & 1u)) st3(B.histories, N, p, hb);
+        mask = nonzero ? (mask | 1u) : (mask & ~1u);
         if (v3_len_sq(jb) > 0.0f) {
             total = v3_add(total, jb);
             board_hit = true;
@@ -259,15 +288,19 @@ __global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
     for (int k = 0; k < P.tool_count; ++k) {
         bm_v3 reaction = v3_zero(), torque = v3_zero();
         if (active) {
-            const ToolF T = load_tool(B.tool_f + 13 * k);
-            total = v3_add(total, blade_at(P, B, p, k, T, cutting, &reaction, &torque, &work));
+            const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
+            total = v3_add(total, blade_at(P, B, p, k, T, cutting, xp, vp, speed, radius_of_blade, &mask, &reaction,
+                                           &torque, &work));
         }
         const bool hit = v3_len_sq(reaction) > 0.0f || v3_len_sq(torque) > 0.0f;
         warp_accumulate3(B.acc + BM_ACC_REACTION(k), reaction, hit);
         warp_accumulate3(B.acc + BM_ACC_TORQUE(k), torque, hit);
     }
     if (__any_sync(0xffffffffu, work.lo != 0u || work.hi != 0u)) warp_accumulate(B.acc + BM_ACC_WORK, work);
-    if (active) st3(B.impulses, N, p, total);
+    if (active) {
+        st3(B.impulses, N, p, total);
+        if (mask != mask_in) B.hist_mask[p] = (uint16_t)mask;
+    }
     // maximum speed: warp max, then one atomic per warp
     for (int d = 16; d > 0; d >>= 1) speed = fmaxf(speed, __shfl_xor_sync(0xffffffffu, speed, d));
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(B.speed, speed);

@@ -54,6 +54,11 @@ __device__ __forceinline__ bm_v3 stencil_g(const bm_buffers& B, int sid, int a) 
 struct ToolF {
     bm_v3 pos, vel, omega;
     bm_q rot;
+    float speed;        // |vel|
+    float spin_reach;   // |omega| * blade radius
+    bm_v3 edge;         // pos + rot (0, 0, -half_z)
+    bm_v3 down;         // rot (0, 0, -1)
+    bm_v3 edge_vel;     // vel + omega x (edge - pos)
 };
 __device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
     ToolF r;
@@ -64,7 +69,15 @@ __device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
     r.rot.z = t[8];
     r.rot.w = t[9];
     r.omega = v3(t[10], t[11], t[12]);
+    r.speed = t[13];
+    r.spin_reach = t[14];
+    r.edge = v3(t[15], t[16], t[17]);
+    r.down = v3(t[18], t[19], t[20]);
+    r.edge_vel = v3(t[21], t[22], t[23]);
     return r;
+}
+__device__ __forceinline__ float blade_radius(const bm_params& P) {
+    return sqrtf((P.half[0] * P.half[0] + P.half[1] * P.half[1]) + P.half[2] * P.half[2]);
 }
 
 // Exact accumulation: warp-sum of 128-bit fixed-point values, then one

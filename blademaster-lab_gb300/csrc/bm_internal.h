@@ -12,6 +12,8 @@ struct bm_solver {
     float* viscous_scratch;  // [9][n] inside B.scratch
     int32_t* scan_partials;  // inside B.scratch
     int64_t buckets;
+    cudaStream_t side;       // knife integration runs here, concurrent with the transfers
+    cudaEvent_t fork, join;
 };
 
 namespace bm {
@@ -21,7 +23,8 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st);
 void launch_g2p(const bm_solver* s, cudaStream_t st);
 void launch_remap(const bm_solver* s, cudaStream_t st);
-void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, cudaStream_t st);
+void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,
+                           cudaStream_t st);
 void launch_refresh_stress(const bm_solver* s, cudaStream_t st);
 void launch_validate(const bm_solver* s, cudaStream_t st);
 void launch_clear_flag(const bm_solver* s, int which, cudaStream_t st);

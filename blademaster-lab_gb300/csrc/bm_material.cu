@@ -4,12 +4,14 @@
 // Layout: particles are sorted by reference cell, so the particles that weigh
 // a grid node are the contents of its eight adjacent cells, contiguous in
 // memory.  The reference scatters (p, a) contributions with float atomics into
-// a hash of (node, code) keys; here every grid slot is produced by one thread
-// that gathers its contributions in ascending particle order, so the sums are
-// deterministic and no float atomic touches the primary fields.  A node's
-// fields (one per distinct cut code among its contributors, ascending code)
-// live at slot f * node_count + node; each particle carries the field index of
-// each of its eight stencil nodes in one uint64 (fidx).
+// a hash of (node, code) keys; here each cell's particles first reduce their
+// contributions to each of the cell's corners with a fixed warp-shuffle tree
+// (cell pass), and one thread per node then adds the partials of its adjacent
+// cells in a fixed order (node pass), so the sums are deterministic and no
+// float atomic touches the primary fields.  A node's fields (one per distinct
+// cut code among its contributors, ascending code) live at slot
+// f * node_count + node; each particle carries the field index of each of its
+// eight stencil nodes in one uint64 (fidx).
 #include "bm_device.cuh"
 #include "bm_internal.h"
 
@@ -37,11 +39,15 @@ __device__ __forceinline__ void for_contributions(const bm_params& P, const bm_b
 
 // Solver._register_topology, node pass: the distinct codes among a node's
 // contributors in ascending order (material.register, material.py:50-66).
+__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n);
+
 __global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
     if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.active_nodes) return;
-    const int n = B.active[t];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P.active_nodes; t += gridDim.x * blockDim.x)
+        register_node(P, B, field_codes, B.active[t]);
+}
+
+__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n) {
     int nf = 0;
     int64_t prev = 0;
     bool have_prev = false;
@@ -74,10 +80,14 @@ __global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __res
 }
 
 // Particle pass: the field index of the particle's code at each stencil node.
+__device__ void register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int p);
+
 __global__ void k_register_particles(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
     if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.n) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) register_particle(P, B, field_codes, p);
+}
+
+__device__ void register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int p) {
     const int64_t code = field_codes[p];
     const int base = B.base_node[p];
     uint64_t fidx = 0u;
@@ -95,37 +105,191 @@ __global__ void k_register_particles(bm_params P, bm_buffers B, const int64_t* _
 __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 
 // ------------------------------------------------------------------- P2G
+//
+// Summation order (shared with the oracle): the contribution of the <= 8
+// particles of a cell to one of its corner nodes is summed by a fixed tree
+// over the cell's 8 particle slots, ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)), with
+// absent particles and particles of another field contributing +0; a node
+// then adds the partials of its adjacent cells in ascending cell index
+// (corner index a = 7 .. 0), skipping cells without a particle of the field.
 
+constexpr int kMixed = 255;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float tree8(float v) {
+    v = v + __shfl_xor_sync(kFull, v, 1);
+    v = v + __shfl_xor_sync(kFull, v, 2);
+    v = v + __shfl_xor_sync(kFull, v, 4);
+    return v;
+}
+__device__ __forceinline__ int group_min(int v) {
+    v = min(v, __shfl_xor_sync(kFull, v, 1));
+    v = min(v, __shfl_xor_sync(kFull, v, 2));
+    return min(v, __shfl_xor_sync(kFull, v, 4));
+}
+__device__ __forceinline__ int group_max(int v) {
+    v = max(v, __shfl_xor_sync(kFull, v, 1));
+    v = max(v, __shfl_xor_sync(kFull, v, 2));
+    return max(v, __shfl_xor_sync(kFull, v, 4));
+}
+__device__ __forceinline__ int cell_count(const bm_params& P) { return P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]; }
+// Node of corner (0, 0, 0) of cell c.
+__device__ __forceinline__ int cell_base_node(const bm_params& P, int c) {
+    const int ck = c % P.cell_dims[2], cj = (c / P.cell_dims[2]) % P.cell_dims[1], ci = c / (P.cell_dims[1] * P.cell_dims[2]);
+    return (ci * P.node_dims[1] + cj) * P.node_dims[2] + ck;
+}
+// The cell whose corner a is node n, or -1.
+__device__ __forceinline__ int cell_at(const bm_params& P, int n, int a) {
+    const int nyz = P.node_dims[1] * P.node_dims[2];
+    const int ci = n / nyz - ((a >> 2) & 1), cj = (n / P.node_dims[2]) % P.node_dims[1] - ((a >> 1) & 1),
+              ck = n % P.node_dims[2] - (a & 1);
+    if (ci < 0 || cj < 0 || ck < 0 || ci >= P.cell_dims[0] || cj >= P.cell_dims[1] || ck >= P.cell_dims[2]) return -1;
+    return (ci * P.cell_dims[1] + cj) * P.cell_dims[2] + ck;
+}
+
+struct P2GContrib {
+    float m;
+    bm_v3 mom, J;
+};
 struct NodeSums {
     float m;
     bm_v3 mom, J;
 };
-
-// material.p2g (material.py:127-152) for field f of node n, ascending particle order.
-__device__ __forceinline__ NodeSums p2g_sums(const bm_params& P, const bm_buffers& B, int n, int f, bool all) {
-    NodeSums s;
-    s.m = 0.0f;
-    s.mom = v3_zero();
-    s.J = v3_zero();
-    const float dtv = P.dt * P.volume;
-    const int64_t N = P.n;
-    for_contributions(P, B, n, [&](int p, int a) {
-        if (!all && field_of(B.fidx[p], a) != f) return;
-        const int sid = B.stencil_id[p];
-        const float w = stencil_w(B, sid, a);
-        const bm_v3 g = stencil_g(B, sid, a);
-        const float mw = P.mass * w;
-        s.m = s.m + mw;
-        s.mom = v3_add(s.mom, v3_mul(ld3(B.v, N, p), mw));
-        const bm_v3 jp = v3_mul(ld3(B.impulses, N, p), w);
-        const bm_v3 sg = m33_mul_v3(m33_scale(ld9(B.stress, N, p), dtv), g);
-        s.J = v3_add(s.J, v3_sub(jp, sg));
-    });
-    return s;
+// One particle's p2g contribution to its corner a (material.py:149-152).
+__device__ __forceinline__ P2GContrib p2g_contrib(const bm_params& P, const bm_buffers& B, bm_v3 v, bm_v3 imp,
+                                                  const bm_m33& scaled_stress, int sid, int a) {
+    const float w = stencil_w(B, sid, a);
+    const bm_v3 g = stencil_g(B, sid, a);
+    P2GContrib c;
+    c.m = P.mass * w;
+    c.mom = v3_mul(v, c.m);
+    c.J = v3_sub(v3_mul(imp, w), m33_mul_v3(scaled_stress, g));
+    return c;
 }
 
-// p2g + couple_and_velocity (material.py:127-152, 252-284), one thread per
-// active node; also clears the topology flag consumed by registration.
+// Cell pass of p2g: thread (cell, slot); per corner a, the 8-slot tree sum
+// written to cell_part[.][a][corner node] with the corner's field (or mixed).
+__global__ void k_p2g_cells(bm_params P, bm_buffers B) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int cells = cell_count(P);
+    const int c = (int)(t >> 3), s = (int)(t & 7);
+    const int64_t N = P.n, NC = P.node_count;
+    int count = 0, p = 0, base = 0;
+    if (c < cells) {
+        const int b = B.cell_start[c];
+        count = B.cell_start[c + 1] - b;
+        p = b + s;
+        base = cell_base_node(P, c);
+    }
+    const bool present = s < count;
+    bm_v3 v = v3_zero(), imp = v3_zero();
+    bm_m33 S = m33_zero();
+    int sid = 0;
+    uint64_t fidx = 0u;
+    if (present) {
+        v = ld3(B.v, N, p);
+        imp = ld3(B.impulses, N, p);
+        S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
+        sid = B.stencil_id[p];
+        fidx = B.fidx[p];
+    }
+#pragma unroll 1
+    for (int a = 0; a < 8; ++a) {
+        P2GContrib k;
+        k.m = 0.0f;
+        k.mom = v3_zero();
+        k.J = v3_zero();
+        int fa = kMixed, fb = 0;
+        if (present) {
+            k = p2g_contrib(P, B, v, imp, S, sid, a);
+            fa = fb = field_of(fidx, a);
+        }
+        const float m = tree8(k.m);
+        const float mx = tree8(k.mom.x), my = tree8(k.mom.y), mz = tree8(k.mom.z);
+        const float jx = tree8(k.J.x), jy = tree8(k.J.y), jz = tree8(k.J.z);
+        const int lo = group_min(fa), hi = group_max(fb);
+        if (s == a && count > 0) {
+            const int64_t node = base + node_offset(P, a);
+            float* part = B.cell_part + a * NC + node;
+            const int64_t plane = 8 * NC;
+            part[0] = m;
+            part[plane] = mx;
+            part[2 * plane] = my;
+            part[3 * plane] = mz;
+            part[4 * plane] = jx;
+            part[5 * plane] = jy;
+            part[6 * plane] = jz;
+            B.cell_field[a * NC + node] = (uint8_t)(lo == hi ? lo : kMixed);
+        }
+    }
+}
+
+// The tree sum of one field f over the particles of cell c at corner a
+// (the mixed-cell path); returns false if no particle of c has field f there.
+__device__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, P2GContrib* out) {
+    const int64_t N = P.n;
+    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+    P2GContrib slot[8];
+    bool any = false;
+    for (int s = 0; s < 8; ++s) {
+        slot[s].m = 0.0f;
+        slot[s].mom = v3_zero();
+        slot[s].J = v3_zero();
+        if (s < count && field_of(B.fidx[b + s], a) == f) {
+            const int p = b + s;
+            slot[s] = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
+                                  m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
+            any = true;
+        }
+    }
+    if (!any) return false;
+    P2GContrib r;
+    r.m = ((slot[0].m + slot[1].m) + (slot[2].m + slot[3].m)) + ((slot[4].m + slot[5].m) + (slot[6].m + slot[7].m));
+#define BM_TREE_V(field)                                                                                        \
+    v3(((slot[0].field.x + slot[1].field.x) + (slot[2].field.x + slot[3].field.x)) +                           \
+           ((slot[4].field.x + slot[5].field.x) + (slot[6].field.x + slot[7].field.x)),                        \
+       ((slot[0].field.y + slot[1].field.y) + (slot[2].field.y + slot[3].field.y)) +                           \
+           ((slot[4].field.y + slot[5].field.y) + (slot[6].field.y + slot[7].field.y)),                        \
+       ((slot[0].field.z + slot[1].field.z) + (slot[2].field.z + slot[3].field.z)) +                           \
+           ((slot[4].field.z + slot[5].field.z) + (slot[6].field.z + slot[7].field.z)))
+    r.mom = BM_TREE_V(mom);
+    r.J = BM_TREE_V(J);
+#undef BM_TREE_V
+    *out = r;
+    return true;
+}
+
+// Node pass of p2g: field sums over the adjacent cells' partials.
+__device__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n, int f) {
+    const int64_t NC = P.node_count, plane = 8 * NC;
+    NodeSums r;
+    r.m = 0.0f;
+    r.mom = v3_zero();
+    r.J = v3_zero();
+#pragma unroll 1
+    for (int a = 7; a >= 0; --a) {
+        const int c = cell_at(P, n, a);
+        if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
+        const int flag = B.cell_field[a * NC + n];
+        if (flag == f) {
+            const float* part = B.cell_part + a * NC + n;
+            r.m = r.m + part[0];
+            r.mom = v3_add(r.mom, v3(part[plane], part[2 * plane], part[3 * plane]));
+            r.J = v3_add(r.J, v3(part[4 * plane], part[5 * plane], part[6 * plane]));
+        } else if (flag == kMixed) {
+            P2GContrib k;
+            if (p2g_mixed(P, B, c, a, f, &k)) {
+                r.m = r.m + k.m;
+                r.mom = v3_add(r.mom, k.mom);
+                r.J = v3_add(r.J, k.J);
+            }
+        }
+    }
+    return r;
+}
+
+// p2g node sums + couple_and_velocity (material.py:127-152, 252-284), one
+// thread per active node; also clears the topology flag consumed by registration.
 __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
@@ -134,7 +298,7 @@ __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     const int nf = B.nfield[n];
     const int64_t S = (int64_t)P.fmax * P.node_count;
     if (nf == 1) {
-        const NodeSums s = p2g_sums(P, B, n, 0, true);
+        const NodeSums s = p2g_node_sums(P, B, n, 0);
         B.grid_mass[n] = s.m;
         if (write_sums) {
             st3(B.momentum, S, n, s.mom);
@@ -152,7 +316,7 @@ __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
         return;
     }
     for (int f = 0; f < nf; ++f) {
-        const NodeSums s = p2g_sums(P, B, n, f, false);
+        const NodeSums s = p2g_node_sums(P, B, n, f);
         const int64_t slot = (int64_t)f * P.node_count + n;
         B.grid_mass[slot] = s.m;
         st3(B.momentum, S, slot, s.mom);
@@ -188,47 +352,102 @@ __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
 
 // ------------------------------------------------------------------- G2P
 
-// material.g2p_at (material.py:343-367) plus the pair-list displacement check
-// of contact.check_pair_list (contact.py:716-735) on the new x, v.
+// material.g2p_at (material.py:343-367), the pair-list displacement check of
+// contact.check_pair_list (contact.py:716-735) on the new x, v, and the cell
+// partials of the MUSL re-scatter (material.py:400-401), thread (cell, slot).
 __global__ void k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.n) return;
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
-    const int sid = B.stencil_id[p], base = B.base_node[p];
-    const uint64_t fidx = B.fidx[p];
-    bm_v3 pic = v3_zero(), dv = v3_zero();
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        const int64_t s = slot_of(P, base, fidx, a);
-        const float w = stencil_w(B, sid, a);
-        const bm_v3 nv = ld3(B.new_v, S, s);
-        pic = v3_add(pic, v3_mul(nv, w));
-        dv = v3_add(dv, v3_mul(v3_sub(nv, ld3(B.old_v, S, s)), w));
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int cells = cell_count(P);
+    const int c = (int)(t >> 3), s = (int)(t & 7);
+    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count, NC = P.node_count;
+    int count = 0, p = 0, base = 0;
+    if (c < cells) {
+        const int b = B.cell_start[c];
+        count = B.cell_start[c + 1] - b;
+        p = b + s;
+        base = cell_base_node(P, c);
     }
-    const bm_v3 v = v3_add(v3_mul(pic, 1.0f - P.flip), v3_mul(v3_add(ld3(B.v, N, p), dv), P.flip));
-    const bm_v3 x = v3_add(ld3(B.x, N, p), v3_mul(pic, P.dt));
-    st3(B.v, N, p, v);
-    st3(B.x, N, p, x);
-    if (check_list) {
-        if (v3_len(v3_sub(x, ld3(B.built_x, N, p))) + P.dt * v3_len(v) > half_skin) B.flags[BM_FLAG_PAIR_DIRTY] = 1;
+    const bool present = s < count;
+    bm_v3 v = v3_zero();
+    int sid = 0;
+    if (present) {
+        sid = B.stencil_id[p];
+        const uint64_t fidx = B.fidx[p];
+        bm_v3 pic = v3_zero(), dv = v3_zero();
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int64_t slot = (int64_t)field_of(fidx, a) * NC + base + node_offset(P, a);
+            const float w = stencil_w(B, sid, a);
+            const bm_v3 nv = ld3(B.new_v, S, slot);
+            pic = v3_add(pic, v3_mul(nv, w));
+            dv = v3_add(dv, v3_mul(v3_sub(nv, ld3(B.old_v, S, slot)), w));
+        }
+        v = v3_add(v3_mul(pic, 1.0f - P.flip), v3_mul(v3_add(ld3(B.v, N, p), dv), P.flip));
+        const bm_v3 x = v3_add(ld3(B.x, N, p), v3_mul(pic, P.dt));
+        st3(B.v, N, p, v);
+        st3(B.x, N, p, x);
+        if (check_list && v3_len(v3_sub(x, ld3(B.built_x, N, p))) + P.dt * v3_len(v) > half_skin)
+            B.flags[BM_FLAG_PAIR_DIRTY] = 1;
+    }
+    const int64_t plane = 8 * NC;
+#pragma unroll 1
+    for (int a = 0; a < 8; ++a) {
+        bm_v3 r = v3_zero();
+        if (present) r = v3_mul(v, P.mass * stencil_w(B, sid, a));
+        const float rx = tree8(r.x), ry = tree8(r.y), rz = tree8(r.z);
+        if (s == a && count > 0) {
+            float* part = B.cell_part + a * NC + base + node_offset(P, a);
+            part[0] = rx;
+            part[plane] = ry;
+            part[2 * plane] = rz;
+        }
     }
 }
 
 // ---------------------------------------------------------- remap + couple
 
-// The MUSL re-scatter of g2p_remap (material.py:397-401) gathered per slot,
-// then couple (material.py:155-193); stores coupled / mass for the F update.
+// Remap sums of field f at node n from the cell partials (mixed cells recomputed).
+__device__ bm_v3 remap_node_sum(const bm_params& P, const bm_buffers& B, int n, int f) {
+    const int64_t N = P.n, NC = P.node_count, plane = 8 * NC;
+    bm_v3 r = v3_zero();
+#pragma unroll 1
+    for (int a = 7; a >= 0; --a) {
+        const int c = cell_at(P, n, a);
+        if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
+        const int flag = B.cell_field[a * NC + n];
+        if (flag == f) {
+            const float* part = B.cell_part + a * NC + n;
+            r = v3_add(r, v3(part[0], part[plane], part[2 * plane]));
+        } else if (flag == kMixed) {
+            const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+            bm_v3 slot[8];
+            bool any = false;
+            for (int s = 0; s < 8; ++s) {
+                slot[s] = v3_zero();
+                if (s < count && field_of(B.fidx[b + s], a) == f) {
+                    slot[s] = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
+                    any = true;
+                }
+            }
+            if (any)
+                r = v3_add(r, v3(((slot[0].x + slot[1].x) + (slot[2].x + slot[3].x)) + ((slot[4].x + slot[5].x) + (slot[6].x + slot[7].x)),
+                                 ((slot[0].y + slot[1].y) + (slot[2].y + slot[3].y)) + ((slot[4].y + slot[5].y) + (slot[6].y + slot[7].y)),
+                                 ((slot[0].z + slot[1].z) + (slot[2].z + slot[3].z)) + ((slot[4].z + slot[5].z) + (slot[6].z + slot[7].z))));
+        }
+    }
+    return r;
+}
+
+// Node pass of the MUSL re-scatter, then couple (material.py:155-193);
+// stores coupled / mass for the F update.
 __global__ void k_remap_couple(bm_params P, bm_buffers B) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     const int nf = B.nfield[n];
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int64_t S = (int64_t)P.fmax * P.node_count;
     if (nf == 1) {
-        bm_v3 r = v3_zero();
-        for_contributions(P, B, n, [&](int p, int a) {
-            r = v3_add(r, v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a)));
-        });
+        const bm_v3 r = remap_node_sum(P, B, n, 0);
         const float m = B.grid_mass[n];
         if (m <= 0.0f) {
             st3(B.remap_v, S, n, v3_zero());
@@ -238,14 +457,7 @@ __global__ void k_remap_couple(bm_params P, bm_buffers B) {
         st3(B.remap_v, S, n, v3_div(coupled, m));
         return;
     }
-    for (int f = 0; f < nf; ++f) {
-        bm_v3 r = v3_zero();
-        for_contributions(P, B, n, [&](int p, int a) {
-            if (field_of(B.fidx[p], a) != f) return;
-            r = v3_add(r, v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a)));
-        });
-        st3(B.remapped, S, (int64_t)f * P.node_count + n, r);
-    }
+    for (int f = 0; f < nf; ++f) st3(B.remapped, S, (int64_t)f * P.node_count + n, remap_node_sum(P, B, n, f));
     for (int f = 0; f < nf; ++f) {
         const int64_t a = (int64_t)f * P.node_count + n;
         const float ma = B.grid_mass[a];
@@ -448,34 +660,42 @@ __global__ void k_plastic_project(float* F, float* Fp, int n, float mu, float yi
 }
 
 // contact.assign (contact.py:996-1039) for every knife, knife k labelling the
-// digit 3^(cut_index + k).
-__device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int cut_index, int cutting) {
+// digit 3^(cut_index + k).  The band tests run before the digit test (both
+// must hold, neither has side effects), so the int64 division only runs for
+// particles in a knife's band.
+__device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int cut_index, int cutting, bm_v3 xp,
+                             bm_v3 vp) {
     if (cutting == 0) return;
-    const int64_t N = P.n;
-    const bm_v3 xp = ld3(B.x, N, p), vp = ld3(B.v, N, p);
-    int64_t code = B.codes[p];
-    bool changed = false;
-    int64_t digit = 1;
-    for (int e = 0; e < cut_index; ++e) digit *= 3;
-    for (int k = 0; k < P.tool_count; ++k, digit *= 3) {
-        if ((code / digit) % 3 != 0) continue;
-        const ToolF T = load_tool(B.tool_f + 13 * k);
-        const bm_v3 edge = v3_add(T.pos, q_rotate(T.rot, v3(0.0f, 0.0f, -P.half[2])));
-        const bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, edge));
+    int64_t code = 0;
+    bool loaded = false, changed = false;
+    const float band = 6.0f * P.spacing;
+    for (int k = 0; k < P.tool_count; ++k) {
+        const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
+        const bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, T.edge));
+        if (!(fabsf(local.x) <= band && fabsf(local.y) <= P.half[1])) continue;
         const float front = -local.z;
-        const bm_v3 edge_v = v3_add(T.vel, v3_cross(T.omega, v3_sub(edge, T.pos)));
-        const bm_v3 d = q_rotate(T.rot, v3(0.0f, 0.0f, -1.0f));
-        const float advance = v3_dot(v3_sub(edge_v, vp), d);
+        const float advance = v3_dot(v3_sub(T.edge_vel, vp), T.down);
         const float back = 2.0f * P.spacing + bm_maxf(advance * P.dt, 0.0f);
         const bool behind = front >= -back && front <= 0.0f;
-        const bool on_board = (P.board_half[0] == 0.0f || fabsf(xp.x) <= P.board_half[0]) &&
-                              (P.board_half[1] == 0.0f || fabsf(xp.y) <= P.board_half[1]);
-        const bm_v3 edge_here = v3_add(edge, q_rotate(T.rot, v3(0.0f, local.y, 0.0f)));
-        const bool pinched = on_board && edge_here.z <= P.radius && xp.z <= edge_here.z + P.radius;
-        if (fabsf(local.x) <= 6.0f * P.spacing && fabsf(local.y) <= P.half[1] && (behind || pinched)) {
-            code += digit * (local.x < 0.0f ? 1 : 2);
-            changed = true;
+        bool pinched = false;
+        if (!behind) {
+            const bool on_board = (P.board_half[0] == 0.0f || fabsf(xp.x) <= P.board_half[0]) &&
+                                  (P.board_half[1] == 0.0f || fabsf(xp.y) <= P.board_half[1]);
+            if (on_board) {
+                const bm_v3 edge_here = v3_add(T.edge, q_rotate(T.rot, v3(0.0f, local.y, 0.0f)));
+                pinched = edge_here.z <= P.radius && xp.z <= edge_here.z + P.radius;
+            }
         }
+        if (!(behind || pinched)) continue;
+        if (!loaded) {
+            code = B.codes[p];
+            loaded = true;
+        }
+        int64_t digit = 1;
+        for (int e = 0; e < cut_index + k; ++e) digit *= 3;
+        if ((code / digit) % 3 != 0) continue;
+        code += digit * (local.x < 0.0f ? 1 : 2);
+        changed = true;
     }
     if (changed) {
         B.codes[p] = code;
@@ -485,9 +705,11 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
 }
 
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
-// with this substep's side labelling (run after the tool update).
-__global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting) {
+// with this substep's side labelling (run after the tool update); thread 0
+// advances the substep counter of the friction-history ping-pong.
+__global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting, int advance_step) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
     if (p >= P.n) return;
     const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
     if (do_update) {
@@ -502,7 +724,7 @@ __global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int c
         st9(B.F, N, p, m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt)));
         constitutive(P, B, p);
     }
-    assign_sides(P, B, p, cut_index, cutting);
+    if (cutting) assign_sides(P, B, p, cut_index, cutting, ld3(B.x, N, p), ld3(B.v, N, p));
 }
 
 // material.validate_interval (material.py:6-20).
@@ -604,8 +826,11 @@ __global__ void k_grid_vel(bm_params P, bm_buffers B, const float* __restrict__ 
 
 void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st) {
     const bm_params& P = s->P;
-    k_register_nodes<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B, field_codes, force);
-    k_register_particles<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, field_codes, force);
+    const unsigned wide = 8 * 152;  // grid-stride: cheap to launch when the gate is off
+    const unsigned gn = grid_for(P.active_nodes) < wide ? grid_for(P.active_nodes) : wide;
+    const unsigned gp = grid_for(P.n) < wide ? grid_for(P.n) : wide;
+    k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes, force);
+    k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes, force);
 }
 
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
@@ -614,6 +839,7 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     const int64_t S = (int64_t)P.fmax * P.node_count;
     if (P.viscous) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
+        k_p2g_cells<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, 1);
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.grid_impulse);
@@ -624,13 +850,15 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.remap_v);
         (void)S;
     } else {
+        k_p2g_cells<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, write_sums);
     }
 }
 
 void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
-    k_g2p<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
+    k_g2p<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(
+        P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
 }
 
 void launch_remap(const bm_solver* s, cudaStream_t st) {
@@ -638,9 +866,10 @@ void launch_remap(const bm_solver* s, cudaStream_t st) {
     k_remap_couple<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B);
 }
 
-void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, cudaStream_t st) {
+void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,
+                           cudaStream_t st) {
     const bm_params& P = s->P;
-    k_fupdate_assign<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, do_update, cut_index, cutting);
+    k_fupdate_assign<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, do_update, cut_index, cutting, advance_step);
 }
 
 void launch_refresh_stress(const bm_solver* s, cudaStream_t st) {

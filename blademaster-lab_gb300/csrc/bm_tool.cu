@@ -26,10 +26,33 @@ __device__ __forceinline__ void dput3(double* t, bm_v3d v) {
     t[2] = v.z;
 }
 
-__device__ void write_mirror(const bm_buffers& B, int k) {
+// Float32 knife record read by the particle kernels; the derived entries are
+// evaluated with the same operations the particle code would apply.
+__device__ void write_mirror(const bm_params& P, const bm_buffers& B, int k) {
     const double* t = B.tool + 13 * k;
-    float* f = B.tool_f + 13 * k;
+    float* f = B.tool_f + BM_TOOL_F_WORDS * k;
     for (int i = 0; i < 13; ++i) f[i] = (float)t[i];
+    const bm_v3 pos = v3(f[0], f[1], f[2]), vel = v3(f[3], f[4], f[5]), omega = v3(f[10], f[11], f[12]);
+    bm_q q;
+    q.x = f[6];
+    q.y = f[7];
+    q.z = f[8];
+    q.w = f[9];
+    f[13] = v3_len(vel);
+    f[14] = v3_len(omega) * blade_radius(P);
+    const bm_v3 edge = v3_add(pos, q_rotate(q, v3(0.0f, 0.0f, -P.half[2])));
+    const bm_v3 down = q_rotate(q, v3(0.0f, 0.0f, -1.0f));
+    const bm_v3 edge_vel = v3_add(vel, v3_cross(omega, v3_sub(edge, pos)));
+    f[15] = edge.x;
+    f[16] = edge.y;
+    f[17] = edge.z;
+    f[18] = down.x;
+    f[19] = down.y;
+    f[20] = down.z;
+    f[21] = edge_vel.x;
+    f[22] = edge_vel.y;
+    f[23] = edge_vel.z;
+    f[24] = 0.0f;
 }
 
 // tool.vertex (tool.py:118-138).
@@ -96,9 +119,11 @@ __device__ void drive_one(const bm_params& P, const bm_buffers& B, int k, int in
     }
     const bm_v3d normal = v3d(0.0, 0.0, 1.0);
     bm_v3d total = v3d(0.0, 0.0, 0.0);
+    bm_v3d rv[10];
+    for (int i = 0; i < 10; ++i) rv[i] = qd_rotate(q, vertex(i, P));
     for (int sweep = 0; sweep < 6; ++sweep)
         for (int i = 0; i < 10; ++i) {
-            const bm_v3d r = qd_rotate(q, vertex(i, P)), corner = v3d_add(x, r);
+            const bm_v3d r = rv[i], corner = v3d_add(x, r);
             if ((P.board_half_d[0] > 0.0 && fabs(corner.x) > P.board_half_d[0]) ||
                 (P.board_half_d[1] > 0.0 && fabs(corner.y) > P.board_half_d[1]))
                 continue;
@@ -139,7 +164,7 @@ __device__ void drive_one(const bm_params& P, const bm_buffers& B, int k, int in
     t[9] = q.w;
     dput3(t + 10, w);
     dput3(B.table_impulse + 3 * k, total);
-    write_mirror(B, k);
+    write_mirror(P, B, k);
 }
 
 // tool.accumulate_reaction (tool.py:6-16): interval sums about the world origin.
@@ -176,7 +201,7 @@ __device__ void finish_external(const bm_params& P, const bm_buffers& B) {
             t[8] = q.z;
             t[9] = q.w;
         }
-        write_mirror(B, 0);
+        write_mirror(P, B, 0);
     }
     acc_clear3(B.acc, BM_ACC_REACTION(0));
     acc_clear3(B.acc, BM_ACC_TORQUE(0));
@@ -202,11 +227,11 @@ __global__ void k_tool(bm_params P, bm_buffers B, int mode, int index, int advan
             B.speed[0] = 0.0f;
         }
     }
-    if (advance_step && k == 0) B.flags[BM_FLAG_STEP] += 1;
+    (void)advance_step;
 }
 
 // tool.load_external_state (tool.py:19-39).
-__global__ void k_load_external(bm_buffers B) {
+__global__ void k_load_external(bm_params P, bm_buffers B) {
     const float* p = B.packed;
     double* t = B.tool;
     for (int i = 0; i < 3; ++i) t[i] = p[i];
@@ -215,7 +240,7 @@ __global__ void k_load_external(bm_buffers B) {
     for (int i = 0; i < 3; ++i) t[10 + i] = p[10 + i];
     for (int i = 0; i < 36; ++i) B.mobility[i] = p[13 + i];
     for (int i = 0; i < 6; ++i) B.interval[i] = 0.0;
-    write_mirror(B, 0);
+    write_mirror(P, B, 0);
 }
 
 // tool.store_interval (tool.py:56-67).
@@ -236,7 +261,7 @@ __global__ void k_record_pose(bm_buffers B, int index) {
 
 __global__ void k_tool_mirror(bm_params P, bm_buffers B) {
     const int k = threadIdx.x;
-    if (k < P.tool_count) write_mirror(B, k);
+    if (k < P.tool_count) write_mirror(P, B, k);
 }
 
 __global__ void k_read_acc(bm_params P, bm_buffers B, float* reaction, float* torque, float* board, float* work) {
@@ -350,7 +375,7 @@ void launch_tool_step(const bm_solver* s, int mode, int target_index, int advanc
 void launch_step_counter(const bm_solver* s, cudaStream_t st) {
     k_tool<<<1, 32, 0, st>>>(s->P, s->B, -1, 0, 1);
 }
-void launch_load_external(const bm_solver* s, cudaStream_t st) { k_load_external<<<1, 1, 0, st>>>(s->B); }
+void launch_load_external(const bm_solver* s, cudaStream_t st) { k_load_external<<<1, 1, 0, st>>>(s->P, s->B); }
 void launch_store_interval(const bm_solver* s, cudaStream_t st) { k_store_interval<<<1, 1, 0, st>>>(s->B); }
 void launch_record_pose(const bm_solver* s, int index, cudaStream_t st) { k_record_pose<<<1, 1, 0, st>>>(s->B, index); }
 void launch_tool_mirror(const bm_solver* s, cudaStream_t st) { k_tool_mirror<<<1, 32, 0, st>>>(s->P, s->B); }

@@ -43,6 +43,9 @@ extern "C" {
 #define BM_CUT_HOLD 4
 
 #define BM_MAX_TOOLS 16
+/* Float32 knife record: pos 3, vel 3, rot 4, omega 3, |vel| 1, |omega| * blade radius 1,
+ * edge centre 3, cutting direction 3, edge velocity 3, padding 1. */
+#define BM_TOOL_F_WORDS 25
 #define BM_PAIR_LANES 64
 
 /* Scalars of one solver: Config (solver.py:12-149) plus the derived
@@ -124,6 +127,8 @@ typedef struct bm_buffers {
     float* new_v;        /* [3][fmax * node_count] */
     float* remapped;     /* [3][fmax * node_count] remapped momentum (multi-field nodes) */
     float* remap_v;      /* [3][fmax * node_count] coupled remapped momentum / mass */
+    float* cell_part;    /* [7][8][node_count] cell-corner partial sums: from the cell whose corner a is node n */
+    uint8_t* cell_field; /* [8][node_count] field index of a uniform cell corner, 255 if its particles differ */
     /* pair contact */
     float* built_x;      /* [3][n] */
     int64_t* built_codes;/* [n] */
@@ -140,7 +145,8 @@ typedef struct bm_buffers {
     int32_t* pair_count; /* [2] */
     /* tool and scalar state */
     double* tool;        /* [tools][13]: pos 3, vel 3, rot xyzw 4, omega 3 */
-    float* tool_f;       /* [tools][13] float32 mirror read by particle kernels */
+    float* tool_f;       /* [tools][BM_TOOL_F_WORDS] float32 mirror read by particle kernels */
+    uint16_t* hist_mask; /* [n] bit 0: board history may be non-zero; bit 1 + k: knife k's */
     float* mobility;     /* [36] */
     uint64_t* acc;       /* 128-bit accumulators, see BM_ACC_* */
     double* interval;    /* [6] interval impulse 3, angular impulse about the world origin 3 */

@@ -75,6 +75,7 @@ typedef struct orc_state {
     int32_t* pair_used;    /* [2][pair_capacity] */
     int32_t* pair_count;   /* [2] */
     int32_t* cell_head;    /* [buckets] scratch */
+    int32_t* cell_start;   /* [cells + 1] particles of each reference cell (device order) */
     int32_t* cell_next;    /* [n] scratch */
     /* tool */
     double* tool;          /* [tools][13] */
@@ -420,7 +421,22 @@ static void grid_vel(orc_state* S, const float* momentum, const float* impulse, 
     }
 }
 
-/* p2g (material.py:127-152) as a per-slot gather in ascending particle order. */
+/* The cell whose corner a is node n, or -1. */
+static int64_t cell_at(const bm_params* P, int64_t n, int a) {
+    int64_t nyz = (int64_t)P->node_dims[1] * P->node_dims[2];
+    int64_t ci = n / nyz - ((a >> 2) & 1), cj = (n / P->node_dims[2]) % P->node_dims[1] - ((a >> 1) & 1),
+            ck = n % P->node_dims[2] - (a & 1);
+    if (ci < 0 || cj < 0 || ck < 0 || ci >= P->cell_dims[0] || cj >= P->cell_dims[1] || ck >= P->cell_dims[2]) return -1;
+    return (ci * P->cell_dims[1] + cj) * P->cell_dims[2] + ck;
+}
+
+/* ((v0+v1)+(v2+v3))+((v4+v5)+(v6+v7)) */
+static float tree8(const float* v) { return ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])); }
+
+/* p2g (material.py:127-152) in the canonical order: per slot, over the
+ * adjacent cells in ascending cell index, the tree sum over the cell's 8
+ * particle slots of the contributions that map to this slot (others +0);
+ * cells without such a contribution are skipped. */
 static void p2g(const bm_params* P, orc_state* S) {
     int64_t s;
     float dtv = P->dt * P->volume;
@@ -428,20 +444,72 @@ static void p2g(const bm_params* P, orc_state* S) {
     for (s = 0; s < S->capacity; ++s) {
         float m = 0.0f;
         bm_v3 mom = v3_zero(), J = v3_zero();
-        int32_t i;
-        for (i = S->slot_start[s]; i < S->slot_start[s + 1]; ++i) {
-            int64_t p = S->contrib[i] / 8;
-            int a = S->contrib[i] % 8;
-            float w = S->weights[8 * p + a];
-            bm_v3 g = ld3(S->gradients, 8 * p + a);
-            float mw = P->mass * w;
-            m = m + mw;
-            mom = v3_add(mom, v3_mul(ld3(S->v, p), mw));
-            J = v3_add(J, v3_sub(v3_mul(ld3(S->impulses, p), w), m33_mul_v3(m33_scale(ld9(S->stress, p), dtv), g)));
+        int64_t n;
+        int a, k;
+        if (S->keys[s] >= 0) {
+            n = S->keys[s] % P->node_count;
+            for (a = 7; a >= 0; --a) {
+                int64_t c = cell_at(P, n, a), b;
+                int count, any = 0;
+                float vm[8], v0[8], v1[8], v2[8], j0[8], j1[8], j2[8];
+                if (c < 0) continue;
+                b = S->cell_start[c];
+                count = S->cell_start[c + 1] - S->cell_start[c];
+                if (count == 0) continue;
+                for (k = 0; k < 8; ++k) {
+                    vm[k] = v0[k] = v1[k] = v2[k] = j0[k] = j1[k] = j2[k] = 0.0f;
+                    if (k < count && S->slots[8 * (b + k) + a] == s) {
+                        int64_t p = b + k;
+                        float w = S->weights[8 * p + a], mw = P->mass * w;
+                        bm_v3 g = ld3(S->gradients, 8 * p + a), mv = v3_mul(ld3(S->v, p), mw);
+                        bm_v3 jv = v3_sub(v3_mul(ld3(S->impulses, p), w), m33_mul_v3(m33_scale(ld9(S->stress, p), dtv), g));
+                        vm[k] = mw; v0[k] = mv.x; v1[k] = mv.y; v2[k] = mv.z; j0[k] = jv.x; j1[k] = jv.y; j2[k] = jv.z;
+                        any = 1;
+                    }
+                }
+                if (!any) continue;
+                m = m + tree8(vm);
+                mom = v3_add(mom, v3(tree8(v0), tree8(v1), tree8(v2)));
+                J = v3_add(J, v3(tree8(j0), tree8(j1), tree8(j2)));
+            }
         }
         S->grid_mass[s] = m;
         st3(S->momentum, s, mom);
         st3(S->grid_impulse, s, J);
+    }
+}
+
+/* The MUSL re-scatter (material.py:400-401) in the same canonical order. */
+static void remap(const bm_params* P, orc_state* S) {
+    int64_t s;
+#pragma omp parallel for schedule(static)
+    for (s = 0; s < S->capacity; ++s) {
+        bm_v3 r = v3_zero();
+        int64_t n;
+        int a, k;
+        if (S->keys[s] >= 0) {
+            n = S->keys[s] % P->node_count;
+            for (a = 7; a >= 0; --a) {
+                int64_t c = cell_at(P, n, a), b;
+                int count, any = 0;
+                float v0[8], v1[8], v2[8];
+                if (c < 0) continue;
+                b = S->cell_start[c];
+                count = S->cell_start[c + 1] - S->cell_start[c];
+                if (count == 0) continue;
+                for (k = 0; k < 8; ++k) {
+                    v0[k] = v1[k] = v2[k] = 0.0f;
+                    if (k < count && S->slots[8 * (b + k) + a] == s) {
+                        int64_t p = b + k;
+                        bm_v3 rv = v3_mul(ld3(S->v, p), P->mass * S->weights[8 * p + a]);
+                        v0[k] = rv.x; v1[k] = rv.y; v2[k] = rv.z;
+                        any = 1;
+                    }
+                }
+                if (any) r = v3_add(r, v3(tree8(v0), tree8(v1), tree8(v2)));
+            }
+        }
+        st3(S->remapped, s, r);
     }
 }
 
@@ -523,18 +591,7 @@ ORC_API void orc_material_step(const bm_params* P, orc_state* S, const int64_t* 
     }
 #pragma omp parallel for schedule(static)
     for (p = 0; p < P->n; ++p) g2p_at(P, S, p);
-    /* remap scatter (material.py:400-401) gathered per slot */
-#pragma omp parallel for schedule(static)
-    for (s = 0; s < S->capacity; ++s) {
-        bm_v3 r = v3_zero();
-        int32_t i;
-        for (i = S->slot_start[s]; i < S->slot_start[s + 1]; ++i) {
-            int64_t q = S->contrib[i] / 8;
-            int a = S->contrib[i] % 8;
-            r = v3_add(r, v3_mul(ld3(S->v, q), P->mass * S->weights[8 * q + a]));
-        }
-        st3(S->remapped, s, r);
-    }
+    remap(P, S);
 #pragma omp parallel for schedule(static)
     for (s = 0; s < S->capacity; ++s) couple(P, S, S->remapped, S->coupled, s);
     {

@@ -59,7 +59,7 @@ _STATE_FIELDS = [
     "x", "v", "ref", "F", "Fp", "stress", "viscous", "codes", "damage", "histories", "impulses", "nodes",
     "weights", "gradients", "keys", "slots", "node_start", "node_slots", "slot_start", "contrib", "grid_mass",
     "momentum", "grid_impulse", "old_v", "new_v", "remapped", "coupled", "pair_keys", "pair_history", "pair_used",
-    "pair_count", "cell_head", "cell_next", "tool", "mobility", "acc", "interval", "table_impulse", "speed",
+    "pair_count", "cell_head", "cell_start", "cell_next", "tool", "mobility", "acc", "interval", "table_impulse", "speed",
     "errors", "flags", "result",
 ]
 
@@ -137,7 +137,7 @@ class OracleSolver:
         self.reference, self.origin, cells = points(cfg.size, cfg.grid_spacing, cfg.shape, cfg.sampling_seed)
         n = self.n = len(self.reference)
         nodes, w, g = stencil(self.reference, self.origin, cfg.grid_spacing, cells)
-        order, _ = cell_sort(self.reference, self.origin, cfg.grid_spacing, cells)
+        order, cell_start = cell_sort(self.reference, self.origin, cfg.grid_spacing, cells)
         self.order = order
         self.rank = np.empty(n, np.int64)
         self.rank[order] = np.arange(n)
@@ -161,6 +161,8 @@ class OracleSolver:
         pair_list = cfg.pair_search in ("list", "auto")
         p = _native.Params()
         p.n, p.node_count, p.tool_count = n, self.node_count, K
+        for i in range(3):
+            p.node_dims[i], p.cell_dims[i] = int(cells[i] + 1), int(cells[i])
         p.pair_capacity = _pow2_at_least(max(64 * n, 16))
         p.tool_model = -1 if cfg.external_tool else int(cfg.free_blade or cfg.pose_servo)
         p.external_tool = int(cfg.external_tool)
@@ -230,6 +232,7 @@ class OracleSolver:
         buckets = _pow2_at_least(max(2 * n, 1024))
         A["cell_head"] = np.zeros(buckets, np.int32)
         A["cell_next"] = np.zeros(n, np.int32)
+        A["cell_start"] = cell_start.astype(np.int32)
         tool = np.zeros((K, 13))
         tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
         tool[:, 9] = 1.0

@@ -143,3 +143,73 @@ def test_pair_contact_impulses_are_equal_and_opposite():
         np.testing.assert_array_equal(gi, c.get("impulses"))
         assert g.pair_count[1].numpy()[0] == 1
         assert np.all(gi[0] == -gi[1]) and np.any(gi[0] != 0)
+
+
+def test_two_free_knives_label_their_own_digits_bitexact():
+    # tests/test_multi_tool.py:9-60 scene
+    cfg = Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005, free_blade=True, tool_count=2,
+                 blade_half_size=(0.0005, 0.025, 0.02))
+    g, c = both(cfg)
+    z = 0.03 + 0.02 + 0.002
+    g.tool_pos.assign([[-0.015, 0.0, z], [0.015, 0.0, z]])
+    g.tool_vel.assign([[0.0, 0.0, -0.6]] * 2)
+    c.set("tool_pos", [[-0.015, 0.0, z], [0.015, 0.0, z]])
+    c.set("tool_vel", [[0.0, 0.0, -0.6]] * 2)
+    for _ in range(60):
+        g.step(cutting=True)
+        c.step(cutting=True)
+    assert_same(g, c)
+    np.testing.assert_array_equal(g.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
+    codes = g.codes.numpy()
+    assert set(np.unique(codes % 3)) == {0, 1, 2} and set(np.unique((codes // 3) % 3)) == {0, 1, 2}
+    np.testing.assert_array_equal(g.tool_damage[1].numpy(), c.get("tool_damage")[1])
+
+
+def test_jittered_bevel_cut_hold_with_plasticity_bitexact():
+    cfg = replace(Config(), sampling_seed=1, grid_spacing=0.006, blade_bevel_height=0.005, cut_hold=True,
+                  cut_work="advance", yield_stress=2000.0, board_half_extent=(0.05, 0.05))
+    g, c = both(cfg)
+    g.tool_pos.assign([[0.001, 0.0, 0.047]])
+    c.set("tool_pos", [[0.001, 0.0, 0.047]])
+    targets = np.column_stack([np.full(40, 0.001), np.zeros(40), np.linspace(0.02, 0.012, 40)])
+    g.advance(targets, cutting=True)
+    c.advance(targets, cutting=True)
+    assert_same(g, c, EXACT + ("Fp",))
+    np.testing.assert_array_equal(g.work.numpy(), c.get("work").astype(np.float32))
+
+
+@pytest.mark.parametrize("mode", ["hold", "predict"])
+def test_external_modes_match_oracle(mode):
+    cfg = replace(Config(), external_tool=True, tool_substep=mode)
+    g, c = both(cfg)
+    mobility = np.diag([2.0, 3.0, 4.0, 10.0, 12.0, 8.0])
+    state = ToolState([0.0, 0.0, 0.047], [0.0, 0.0, 0.0, 1.0], [0.0, 0.0, -0.05], [0.0, 0.0, 0.1], mobility)
+    port = ExternalToolPort(g)
+    checked = state.checked()
+    packed = np.concatenate([checked.position, checked.orientation_xyzw, checked.linear_velocity,
+                             checked.angular_velocity, checked.mobility.ravel()]).astype(np.float32)
+    for i in range(4):
+        r = port.advance(state, 4 * cfg.dt, cutting=True, cut_index=0)
+        imp, ang, err = c.external_interval(packed, 4, cutting=True)
+        np.testing.assert_array_equal(r.impulse_ns, imp)
+    assert_same(g, c)
+    np.testing.assert_array_equal(g.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
+
+
+def test_single_field_baseline_bitexact():
+    # tests/test_single_field.py:7-21 scene
+    cfg = Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005)
+    g, c = both(cfg)
+    left = g.reference[:, 0] < 0
+    codes = np.where(left, 1, 2).astype(np.int64)
+    v = np.zeros((g.n, 3), np.float32)
+    v[left, 0] = -0.2
+    g.codes.assign(codes), g.v.assign(v)
+    c.set("codes", codes), c.set("v", v)
+    g.set_single_field(True)
+    c.single_field = True
+    for _ in range(10):
+        g.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
+        c.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
+    assert_same(g, c)
+    assert g.v.numpy()[~left, 0].mean() < -0.01
