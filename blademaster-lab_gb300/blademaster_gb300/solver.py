@@ -252,7 +252,7 @@ class Solver:
         for name in ("momentum", "grid_impulse", "old_v", "new_v", "remapped", "remap_v"):
             T[name] = zeros(3, S)
         T["cell_part"] = zeros(7, 8, self.node_count)
-        T["cell_field"] = zeros(8, self.node_count, dtype=t.uint8)
+        T["cell_field"] = t.as_tensor(self._absent_corners(cell_start), device=dev)
         T["hist_mask"] = t.full((n,), -1, dtype=t.int16, device=dev)
         T["built_x"] = zeros(3, n)
         T["built_codes"] = zeros(n, dtype=i64)
@@ -267,6 +267,10 @@ class Solver:
         T["pair_history"] = zeros(2, self.pair_capacity, 3)
         T["pair_used"] = zeros(2, self.pair_capacity, dtype=i32)
         T["pair_count"] = zeros(2, dtype=i32)
+        T["changed"] = zeros(n, dtype=i32)
+        T["relist"] = zeros(n, dtype=i32)
+        T["relist_list"] = zeros(n, dtype=i32)
+        T["listed"] = zeros(n, dtype=i32)
         tool = np.zeros((K, 13))
         tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
         tool[:, 9] = 1.0
@@ -300,6 +304,25 @@ class Solver:
         self._batches = {}
         self.graph_build_s = 0.0
         self.refresh_stress()
+
+    def _absent_corners(self, cell_start):
+        """cell_field with 254 where node n has no (non-empty) cell at corner a.
+
+        Particles never change reference cell, so this is set once; the cell
+        pass overwrites the other entries every substep.
+        """
+        dims = self.node_dims
+        ijk = np.stack(np.unravel_index(np.arange(self.node_count), tuple(dims)), axis=1)
+        counts = np.diff(cell_start)
+        field = np.full((8, self.node_count), 254, np.uint8)
+        for a, offset in enumerate(OFFSETS):
+            c = ijk - offset
+            inside = np.all((c >= 0) & (c < self.cells), axis=1)
+            linear = np.ravel_multi_index(c[inside].T, tuple(self.cells))
+            occupied = np.zeros(self.node_count, bool)
+            occupied[np.flatnonzero(inside)[counts[linear] > 0]] = True
+            field[a][occupied] = 0
+        return field
 
     # ------------------------------------------------------------ binding
 

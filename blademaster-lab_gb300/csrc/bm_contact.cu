@@ -189,15 +189,22 @@ __device__ bm_v3 blade_at(const bm_params& P, const bm_buffers& B, int p, int k,
     *reaction = v3_zero();
     *torque = v3_zero();
     const float max_closing = (vlen + T.speed) + T.spin_reach;
-    bool far = v3_len(v3_sub(xp, T.pos)) - radius_of_blade - P.blade_offset > P.dt * max_closing;
+    const bm_v3 d = v3_sub(xp, T.pos);
+    bool far = v3_len(d) - radius_of_blade - P.blade_offset > P.dt * max_closing;
     bm_v3 local = v3_zero();
     if (!far) {
-        local = q_rotate_inv(T.rot, v3_sub(xp, T.pos));
         // Contact needs every |local_i| <= half_i + offset + dt * max_closing;
-        // the margin is widened to cover rounding of the exact test below.
+        // the margin is widened to cover rounding of the exact test below, and
+        // the axis projections (a cheaper route to local) get 10 ppm more.
         const float margin = (P.blade_offset + P.dt * max_closing) * 1.01f + 1.0e-6f;
-        far = fabsf(local.x) - P.half[0] > margin || fabsf(local.y) - P.half[1] > margin ||
-              fabsf(local.z) - P.half[2] > margin;
+        const float axis_margin = margin + 1.0e-5f * radius_of_blade;
+        far = fabsf(v3_dot(d, T.ax)) - P.half[0] > axis_margin || fabsf(v3_dot(d, T.ay)) - P.half[1] > axis_margin ||
+              fabsf(v3_dot(d, T.az)) - P.half[2] > axis_margin;
+        if (!far) {
+            local = q_rotate_inv(T.rot, d);
+            far = fabsf(local.x) - P.half[0] > margin || fabsf(local.y) - P.half[1] > margin ||
+                  fabsf(local.z) - P.half[2] > margin;
+        }
     }
     if (far) {
         if (*mask & bit) {
@@ -433,6 +440,7 @@ __global__ void k_pair_setup(bm_params P, bm_buffers B, float* reach_out, int fo
     *reach_out = value;
     B.flags[BM_FLAG_CANDIDATES] = 0;
     B.flags[BM_FLAG_PAIR_BUILDS] += 1;
+    B.flags[BM_FLAG_CHANGED] = 0;  // a full build uses the current codes
 }
 
 __global__ void k_zero_i32(int32_t* a, int64_t n, const int32_t* gate_flag) {
@@ -513,7 +521,7 @@ __global__ void k_bin_scatter(bm_params P, bm_buffers B, const int32_t* gate_fla
     }
 }
 
-__device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float reach);
+__device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float reach, const float* __restrict__ pos);
 __device__ void pair_particle(const bm_params& P, const bm_buffers& B, int p, float reach);
 
 // contact.build_pair_list (contact.py:778-822): partners on both sides within
@@ -521,14 +529,14 @@ __device__ void pair_particle(const bm_params& P, const bm_buffers& B, int p, fl
 __global__ void k_build_lists(bm_params P, bm_buffers B, const float* reach_in, const int32_t* gate_flag) {
     if (gate_flag && *gate_flag == 0) return;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x)
-        build_list(P, B, p, *reach_in);
+        build_list(P, B, p, *reach_in, B.x);
 }
 
-__device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float reach) {
-    const int64_t N = P.n;
-    const bm_v3 xp = ld3(B.x, N, p), rp = ld3(B.ref, N, p);
+__device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float reach, const float* __restrict__ pos) {
+    const int N = P.n;
+    const bm_v3 xp = ld3(pos, N, p), rp = ld3(B.ref, N, p);
     const int64_t cp = B.codes[p];
-    st3(B.built_x, N, p, xp);
+    if (pos == B.x) st3(B.built_x, N, p, xp);
     B.built_codes[p] = cp;
     const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
     int32_t* list = B.partners + (int64_t)p * BM_PAIR_LANES;
@@ -540,7 +548,7 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
         for (int it = begin; it < end; ++it) {
             const int q = B.bucket_items[it];
             if (q == p) continue;
-            const bm_v3 xq = ld3(B.x, N, q);
+            const bm_v3 xq = ld3(pos, N, q);
             if (cell_coord(xq.x, reach) != cx || cell_coord(xq.y, reach) != cy || cell_coord(xq.z, reach) != cz) continue;
             if (!(v3_len(v3_sub(xq, xp)) < reach)) continue;
             if (compatible_codes(cp, B.codes[q]) && v3_len(v3_sub(rp, ld3(B.ref, N, q))) < 2.0f * P.spacing) continue;
@@ -558,10 +566,56 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
         }
     }
     B.partner_count[p] = count;
-    if (count != 0) {
+    if (pos == B.x) B.listed[p] = 0;
+    if (count != 0 && B.listed[p] == 0) {
+        B.listed[p] = 1;
         const int at = atomicAdd(&B.flags[BM_FLAG_CANDIDATES], 1);
         if (at < P.candidate_capacity) B.candidates[at] = p;
     }
+}
+
+// Cut codes changed since the last list update: mark each changed particle
+// and every particle within the build reach of it (build positions and
+// buckets), so their lists are recomputed with the new codes.  Codes only
+// gain digits, so compatibility only turns false and lists only grow; the
+// positions are still within half a skin of the build (else a full build ran).
+__global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in) {
+    const int changed = min(B.flags[BM_FLAG_CHANGED], P.n);
+    if (changed == 0) return;
+    const int N = P.n;
+    const float reach = *reach_in;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < changed; t += gridDim.x * blockDim.x) {
+        const int p = B.changed[t];
+        const bm_v3 xp = ld3(B.built_x, N, p);
+        const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
+        if (atomicExch(&B.relist[p], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = p;
+        for (int i = 0; i < 27; ++i) {
+            const int cx = hx + i % 3 - 1, cy = hy + (i / 3) % 3 - 1, cz = hz + i / 9 - 1;
+            const int b = list_bucket(cx, cy, cz, P.bucket_mask);
+            for (int it = B.bucket_start[b]; it < B.bucket_start[b + 1]; ++it) {
+                const int q = B.bucket_items[it];
+                const bm_v3 xq = ld3(B.built_x, N, q);
+                if (cell_coord(xq.x, reach) != cx || cell_coord(xq.y, reach) != cy || cell_coord(xq.z, reach) != cz) continue;
+                if (!(v3_len(v3_sub(xq, xp)) < reach)) continue;
+                if (atomicExch(&B.relist[q], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = q;
+            }
+        }
+    }
+}
+
+__global__ void k_relist(bm_params P, bm_buffers B, const float* reach_in) {
+    const int count = min(B.flags[BM_FLAG_RELIST], P.n);
+    if (count == 0) return;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int p = B.relist_list[t];
+        build_list(P, B, p, *reach_in, B.built_x);
+        B.relist[p] = 0;
+    }
+}
+
+__global__ void k_relist_done(bm_buffers B) {
+    B.flags[BM_FLAG_CHANGED] = 0;
+    B.flags[BM_FLAG_RELIST] = 0;
 }
 
 // contact.pairs_listed (contact.py:825-925): each candidate adds its pair
@@ -725,7 +779,12 @@ void launch_pairs(const bm_solver* s, cudaStream_t st) {
     k_scan_add<<<gb, kBlock, 0, st>>>(B.bucket_start, buckets, partials, gate);
     k_bin_scatter<<<gn, kBlock, 0, st>>>(P, B, gate);
     k_build_lists<<<gn, kBlock, 0, st>>>(P, B, reach, gate);
-    if (!force) launch_clear_flag(s, BM_FLAG_PAIR_DIRTY, st);
+    if (!force) {
+        launch_clear_flag(s, BM_FLAG_PAIR_DIRTY, st);
+        k_relist_mark<<<152, kBlock, 0, st>>>(P, B, reach);
+        k_relist<<<152, kBlock, 0, st>>>(P, B, reach);
+        k_relist_done<<<1, 1, 0, st>>>(B);
+    }
     const unsigned gc = grid_for(P.candidate_capacity) < wide ? grid_for(P.candidate_capacity) : wide;
     k_pairs<<<gc, kBlock, 0, st>>>(P, B, reach);
 }

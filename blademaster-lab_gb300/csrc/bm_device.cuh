@@ -14,15 +14,17 @@ namespace bm {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ bm_v3 ld3(const float* __restrict__ a, int64_t n, int64_t i) {
+// Structure-of-arrays access with 32-bit indices (every array here holds
+// fewer than 2^31 elements: n < 2^28 particles, fmax * node_count < 2^29).
+__device__ __forceinline__ bm_v3 ld3(const float* __restrict__ a, int n, int i) {
     return v3(a[i], a[n + i], a[2 * n + i]);
 }
-__device__ __forceinline__ void st3(float* __restrict__ a, int64_t n, int64_t i, bm_v3 v) {
+__device__ __forceinline__ void st3(float* __restrict__ a, int n, int i, bm_v3 v) {
     a[i] = v.x;
     a[n + i] = v.y;
     a[2 * n + i] = v.z;
 }
-__device__ __forceinline__ bm_m33 ld9(const float* __restrict__ a, int64_t n, int64_t i) {
+__device__ __forceinline__ bm_m33 ld9(const float* __restrict__ a, int n, int i) {
     bm_m33 m;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -30,7 +32,7 @@ __device__ __forceinline__ bm_m33 ld9(const float* __restrict__ a, int64_t n, in
         for (int c = 0; c < 3; ++c) m.m[r][c] = a[(3 * r + c) * n + i];
     return m;
 }
-__device__ __forceinline__ void st9(float* __restrict__ a, int64_t n, int64_t i, const bm_m33& m) {
+__device__ __forceinline__ void st9(float* __restrict__ a, int n, int i, const bm_m33& m) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -42,8 +44,8 @@ __device__ __forceinline__ int node_offset(const bm_params& P, int a) {
     return ((a >> 2) & 1) * P.node_dims[1] * P.node_dims[2] + ((a >> 1) & 1) * P.node_dims[2] + (a & 1);
 }
 __device__ __forceinline__ int field_of(uint64_t fidx, int a) { return (int)((fidx >> (8 * a)) & 0xffu); }
-__device__ __forceinline__ int64_t slot_of(const bm_params& P, int base, uint64_t fidx, int a) {
-    return (int64_t)field_of(fidx, a) * P.node_count + base + node_offset(P, a);
+__device__ __forceinline__ int slot_of(const bm_params& P, int base, uint64_t fidx, int a) {
+    return field_of(fidx, a) * P.node_count + base + node_offset(P, a);
 }
 __device__ __forceinline__ float stencil_w(const bm_buffers& B, int sid, int a) { return __ldg(&B.stencil_w[8 * sid + a]); }
 __device__ __forceinline__ bm_v3 stencil_g(const bm_buffers& B, int sid, int a) {
@@ -59,6 +61,7 @@ struct ToolF {
     bm_v3 edge;         // pos + rot (0, 0, -half_z)
     bm_v3 down;         // rot (0, 0, -1)
     bm_v3 edge_vel;     // vel + omega x (edge - pos)
+    bm_v3 ax, ay, az;   // knife axes in the world (for conservative pre-tests only)
 };
 __device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
     ToolF r;
@@ -74,6 +77,9 @@ __device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
     r.edge = v3(t[15], t[16], t[17]);
     r.down = v3(t[18], t[19], t[20]);
     r.edge_vel = v3(t[21], t[22], t[23]);
+    r.ax = v3(t[24], t[25], t[26]);
+    r.ay = v3(t[27], t[28], t[29]);
+    r.az = v3(t[30], t[31], t[32]);
     return r;
 }
 __device__ __forceinline__ float blade_radius(const bm_params& P) {

@@ -66,7 +66,7 @@ __device__ void register_node(const bm_params& P, const bm_buffers& B, const int
             atomicAdd(&B.errors[0], 1);
             break;
         }
-        const int64_t s = (int64_t)nf * P.node_count + n;
+        const int s = nf * P.node_count + n;
         B.fcode[s] = best;
         uint64_t ones, twos;
         digit_masks(best, &ones, &twos);
@@ -113,31 +113,44 @@ __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 // then adds the partials of its adjacent cells in ascending cell index
 // (corner index a = 7 .. 0), skipping cells without a particle of the field.
 
-constexpr int kMixed = 255;
+constexpr int kMixed = 255;   // the cell's particles map to different fields at this corner
+constexpr int kAbsent = 254;  // no cell (outside the grid, or empty): set once at setup
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ float tree8(float v) {
-    v = v + __shfl_xor_sync(kFull, v, 1);
-    v = v + __shfl_xor_sync(kFull, v, 2);
-    v = v + __shfl_xor_sync(kFull, v, 4);
-    return v;
-}
-__device__ __forceinline__ int group_min(int v) {
-    v = min(v, __shfl_xor_sync(kFull, v, 1));
-    v = min(v, __shfl_xor_sync(kFull, v, 2));
-    return min(v, __shfl_xor_sync(kFull, v, 4));
-}
-__device__ __forceinline__ int group_max(int v) {
-    v = max(v, __shfl_xor_sync(kFull, v, 1));
-    v = max(v, __shfl_xor_sync(kFull, v, 2));
-    return max(v, __shfl_xor_sync(kFull, v, 4));
+// Reduce-scatter over the 8 lanes of a cell group: vals[c][v] holds this
+// lane's contribution to corner c; on return out[v] holds, in lane s, the sum
+// over the group for corner s.  Each sum is the tree
+// ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)) over the group's lanes (each addition
+// commutes), with 7 V shuffles instead of 24 V for a full butterfly per corner.
+template <int V>
+__device__ __forceinline__ void reduce_scatter8(const float (&vals)[8][V], float (&out)[V]) {
+    const int s = threadIdx.x & 7;
+    const bool b0 = s & 1, b1 = (s >> 1) & 1, b2 = (s >> 2) & 1;
+    float k1[4][V], k2[2][V];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float mine = b0 ? vals[2 * j + 1][v] : vals[2 * j][v];
+            const float other = b0 ? vals[2 * j][v] : vals[2 * j + 1][v];
+            k1[j][v] = mine + __shfl_xor_sync(kFull, other, 1);
+        }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float mine = b1 ? k1[2 * i + 1][v] : k1[2 * i][v];
+            const float other = b1 ? k1[2 * i][v] : k1[2 * i + 1][v];
+            k2[i][v] = mine + __shfl_xor_sync(kFull, other, 2);
+        }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const float mine = b2 ? k2[1][v] : k2[0][v];
+        const float other = b2 ? k2[0][v] : k2[1][v];
+        out[v] = mine + __shfl_xor_sync(kFull, other, 4);
+    }
 }
 __device__ __forceinline__ int cell_count(const bm_params& P) { return P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]; }
-// Node of corner (0, 0, 0) of cell c.
-__device__ __forceinline__ int cell_base_node(const bm_params& P, int c) {
-    const int ck = c % P.cell_dims[2], cj = (c / P.cell_dims[2]) % P.cell_dims[1], ci = c / (P.cell_dims[1] * P.cell_dims[2]);
-    return (ci * P.node_dims[1] + cj) * P.node_dims[2] + ck;
-}
 // The cell whose corner a is node n, or -1.
 __device__ __forceinline__ int cell_at(const bm_params& P, int n, int a) {
     const int nyz = P.node_dims[1] * P.node_dims[2];
@@ -167,67 +180,74 @@ __device__ __forceinline__ P2GContrib p2g_contrib(const bm_params& P, const bm_b
     return c;
 }
 
-// Cell pass of p2g: thread (cell, slot); per corner a, the 8-slot tree sum
+// Cell pass of p2g: thread (cell, slot); the 8-slot tree sums of every corner
 // written to cell_part[.][a][corner node] with the corner's field (or mixed).
-__global__ void k_p2g_cells(bm_params P, bm_buffers B) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int cells = cell_count(P);
-    const int c = (int)(t >> 3), s = (int)(t & 7);
-    const int64_t N = P.n, NC = P.node_count;
-    int count = 0, p = 0, base = 0;
+    const int c = t >> 3, s = t & 7;
+    const int N = P.n, NC = P.node_count;
+    int count = 0, p = 0;
     if (c < cells) {
         const int b = B.cell_start[c];
         count = B.cell_start[c + 1] - b;
         p = b + s;
-        base = cell_base_node(P, c);
     }
     const bool present = s < count;
-    bm_v3 v = v3_zero(), imp = v3_zero();
-    bm_m33 S = m33_zero();
-    int sid = 0;
+    float vals[8][7];
+    int base = 0;
     uint64_t fidx = 0u;
     if (present) {
-        v = ld3(B.v, N, p);
-        imp = ld3(B.impulses, N, p);
-        S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
-        sid = B.stencil_id[p];
+        const bm_v3 v = ld3(B.v, N, p), imp = ld3(B.impulses, N, p);
+        const bm_m33 S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
+        const int sid = B.stencil_id[p];
         fidx = B.fidx[p];
+        base = B.base_node[p];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const P2GContrib k = p2g_contrib(P, B, v, imp, S, sid, a);
+            vals[a][0] = k.m;
+            vals[a][1] = k.mom.x;
+            vals[a][2] = k.mom.y;
+            vals[a][3] = k.mom.z;
+            vals[a][4] = k.J.x;
+            vals[a][5] = k.J.y;
+            vals[a][6] = k.J.z;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int v = 0; v < 7; ++v) vals[a][v] = 0.0f;
     }
-#pragma unroll 1
-    for (int a = 0; a < 8; ++a) {
-        P2GContrib k;
-        k.m = 0.0f;
-        k.mom = v3_zero();
-        k.J = v3_zero();
-        int fa = kMixed, fb = 0;
-        if (present) {
-            k = p2g_contrib(P, B, v, imp, S, sid, a);
-            fa = fb = field_of(fidx, a);
+    float sum[7];
+    reduce_scatter8<7>(vals, sum);
+    // the field of this lane's corner (a = s) over the group's particles
+    const int group = threadIdx.x & ~7;
+    int lo = kMixed, hi = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t fk = __shfl_sync(kFull, fidx, group + k);
+        if (k < count) {
+            const int f = field_of(fk, s);
+            lo = min(lo, f);
+            hi = max(hi, f);
         }
-        const float m = tree8(k.m);
-        const float mx = tree8(k.mom.x), my = tree8(k.mom.y), mz = tree8(k.mom.z);
-        const float jx = tree8(k.J.x), jy = tree8(k.J.y), jz = tree8(k.J.z);
-        const int lo = group_min(fa), hi = group_max(fb);
-        if (s == a && count > 0) {
-            const int64_t node = base + node_offset(P, a);
-            float* part = B.cell_part + a * NC + node;
-            const int64_t plane = 8 * NC;
-            part[0] = m;
-            part[plane] = mx;
-            part[2 * plane] = my;
-            part[3 * plane] = mz;
-            part[4 * plane] = jx;
-            part[5 * plane] = jy;
-            part[6 * plane] = jz;
-            B.cell_field[a * NC + node] = (uint8_t)(lo == hi ? lo : kMixed);
-        }
+    }
+    base = __shfl_sync(kFull, base, group);  // lane 0 of the group is present when count > 0
+    if (count > 0) {
+        const int node = base + node_offset(P, s), plane = 8 * NC;
+        float* part = B.cell_part + s * NC + node;
+#pragma unroll
+        for (int v = 0; v < 7; ++v) part[v * plane] = sum[v];
+        B.cell_field[s * NC + node] = (uint8_t)(lo == hi ? lo : kMixed);
     }
 }
 
-// The tree sum of one field f over the particles of cell c at corner a
-// (the mixed-cell path); returns false if no particle of c has field f there.
-__device__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, P2GContrib* out) {
-    const int64_t N = P.n;
+// The tree sum of field f over the particles of cell c at corner a (a cell
+// whose particles map to different fields there); false if none has f.
+__device__ __noinline__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, P2GContrib* out) {
+    const int N = P.n;
     const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
     P2GContrib slot[8];
     bool any = false;
@@ -259,17 +279,16 @@ __device__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, int c, int a,
     return true;
 }
 
-// Node pass of p2g: field sums over the adjacent cells' partials.
-__device__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n, int f) {
-    const int64_t NC = P.node_count, plane = 8 * NC;
+// Node pass of p2g: field sums over the adjacent cells' partials, in
+// ascending cell index (a = 7 .. 0).
+__device__ __forceinline__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n, int f) {
+    const int NC = P.node_count, plane = 8 * NC;
     NodeSums r;
     r.m = 0.0f;
     r.mom = v3_zero();
     r.J = v3_zero();
-#pragma unroll 1
+#pragma unroll
     for (int a = 7; a >= 0; --a) {
-        const int c = cell_at(P, n, a);
-        if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
         const int flag = B.cell_field[a * NC + n];
         if (flag == f) {
             const float* part = B.cell_part + a * NC + n;
@@ -278,7 +297,7 @@ __device__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n
             r.J = v3_add(r.J, v3(part[4 * plane], part[5 * plane], part[6 * plane]));
         } else if (flag == kMixed) {
             P2GContrib k;
-            if (p2g_mixed(P, B, c, a, f, &k)) {
+            if (p2g_mixed(P, B, cell_at(P, n, a), a, f, &k)) {
                 r.m = r.m + k.m;
                 r.mom = v3_add(r.mom, k.mom);
                 r.J = v3_add(r.J, k.J);
@@ -288,42 +307,18 @@ __device__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n
     return r;
 }
 
-// p2g node sums + couple_and_velocity (material.py:127-152, 252-284), one
-// thread per active node; also clears the topology flag consumed by registration.
-__global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
-    if (t >= P.active_nodes) return;
-    const int n = B.active[t];
-    const int nf = B.nfield[n];
-    const int64_t S = (int64_t)P.fmax * P.node_count;
-    if (nf == 1) {
-        const NodeSums s = p2g_node_sums(P, B, n, 0);
-        B.grid_mass[n] = s.m;
-        if (write_sums) {
-            st3(B.momentum, S, n, s.mom);
-            st3(B.grid_impulse, S, n, s.J);
-        }
-        if (s.m <= 0.0f) {
-            st3(B.old_v, S, n, v3_zero());
-            st3(B.new_v, S, n, v3_zero());
-            return;
-        }
-        const bm_v3 pm = v3_add(s.mom, v3_div(v3_zero(), s.m));
-        const bm_v3 jm = v3_add(s.J, v3_div(v3_zero(), s.m));
-        st3(B.old_v, S, n, v3_div(pm, s.m));
-        st3(B.new_v, S, n, v3_div(v3_add(pm, jm), s.m));
-        return;
-    }
+// Exchange of a node with several fields (material.py:252-284).
+__device__ __noinline__ void p2g_multi_field(const bm_params& P, const bm_buffers& B, int n, int nf) {
+    const int S = P.fmax * P.node_count;
     for (int f = 0; f < nf; ++f) {
         const NodeSums s = p2g_node_sums(P, B, n, f);
-        const int64_t slot = (int64_t)f * P.node_count + n;
+        const int slot = f * P.node_count + n;
         B.grid_mass[slot] = s.m;
         st3(B.momentum, S, slot, s.mom);
         st3(B.grid_impulse, S, slot, s.J);
     }
     for (int f = 0; f < nf; ++f) {
-        const int64_t a = (int64_t)f * P.node_count + n;
+        const int a = f * P.node_count + n;
         const float ma = B.grid_mass[a];
         if (ma <= 0.0f) {
             st3(B.old_v, S, a, v3_zero());
@@ -335,7 +330,7 @@ __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
         float total = 0.0f;
         bm_v3 dm = v3_zero(), di = v3_zero();
         for (int g = 0; g < nf; ++g) {
-            const int64_t b = (int64_t)g * P.node_count + n;
+            const int b = g * P.node_count + n;
             const float mb = B.grid_mass[b];
             total = total + mb;
             if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b])) {
@@ -350,116 +345,143 @@ __global__ void k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     }
 }
 
+// p2g node sums + couple_and_velocity (material.py:127-152, 252-284), one
+// thread per active node; also clears the topology flag consumed by registration.
+__global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int S = P.fmax * P.node_count;
+    if (nf != 1) {
+        p2g_multi_field(P, B, n, nf);
+        return;
+    }
+    const NodeSums s = p2g_node_sums(P, B, n, 0);
+    B.grid_mass[n] = s.m;
+    if (write_sums) {
+        st3(B.momentum, S, n, s.mom);
+        st3(B.grid_impulse, S, n, s.J);
+    }
+    if (s.m <= 0.0f) {
+        st3(B.old_v, S, n, v3_zero());
+        st3(B.new_v, S, n, v3_zero());
+        return;
+    }
+    const bm_v3 pm = v3_add(s.mom, v3_div(v3_zero(), s.m));
+    const bm_v3 jm = v3_add(s.J, v3_div(v3_zero(), s.m));
+    st3(B.old_v, S, n, v3_div(pm, s.m));
+    st3(B.new_v, S, n, v3_div(v3_add(pm, jm), s.m));
+}
+
 // ------------------------------------------------------------------- G2P
 
 // material.g2p_at (material.py:343-367), the pair-list displacement check of
 // contact.check_pair_list (contact.py:716-735) on the new x, v, and the cell
 // partials of the MUSL re-scatter (material.py:400-401), thread (cell, slot).
-__global__ void k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int cells = cell_count(P);
-    const int c = (int)(t >> 3), s = (int)(t & 7);
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count, NC = P.node_count;
-    int count = 0, p = 0, base = 0;
+    const int c = t >> 3, s = t & 7;
+    const int N = P.n, S = P.fmax * P.node_count, NC = P.node_count;
+    int count = 0, p = 0;
     if (c < cells) {
         const int b = B.cell_start[c];
         count = B.cell_start[c + 1] - b;
         p = b + s;
-        base = cell_base_node(P, c);
     }
     const bool present = s < count;
-    bm_v3 v = v3_zero();
-    int sid = 0;
+    float vals[8][3];
+    int base = 0;
     if (present) {
-        sid = B.stencil_id[p];
+        const int sid = B.stencil_id[p];
         const uint64_t fidx = B.fidx[p];
+        base = B.base_node[p];
         bm_v3 pic = v3_zero(), dv = v3_zero();
+        float w[8];
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
-            const int64_t slot = (int64_t)field_of(fidx, a) * NC + base + node_offset(P, a);
-            const float w = stencil_w(B, sid, a);
+            const int slot = field_of(fidx, a) * NC + base + node_offset(P, a);
+            w[a] = stencil_w(B, sid, a);
             const bm_v3 nv = ld3(B.new_v, S, slot);
-            pic = v3_add(pic, v3_mul(nv, w));
-            dv = v3_add(dv, v3_mul(v3_sub(nv, ld3(B.old_v, S, slot)), w));
+            pic = v3_add(pic, v3_mul(nv, w[a]));
+            dv = v3_add(dv, v3_mul(v3_sub(nv, ld3(B.old_v, S, slot)), w[a]));
         }
-        v = v3_add(v3_mul(pic, 1.0f - P.flip), v3_mul(v3_add(ld3(B.v, N, p), dv), P.flip));
+        const bm_v3 v = v3_add(v3_mul(pic, 1.0f - P.flip), v3_mul(v3_add(ld3(B.v, N, p), dv), P.flip));
         const bm_v3 x = v3_add(ld3(B.x, N, p), v3_mul(pic, P.dt));
         st3(B.v, N, p, v);
         st3(B.x, N, p, x);
         if (check_list && v3_len(v3_sub(x, ld3(B.built_x, N, p))) + P.dt * v3_len(v) > half_skin)
             B.flags[BM_FLAG_PAIR_DIRTY] = 1;
-    }
-    const int64_t plane = 8 * NC;
-#pragma unroll 1
-    for (int a = 0; a < 8; ++a) {
-        bm_v3 r = v3_zero();
-        if (present) r = v3_mul(v, P.mass * stencil_w(B, sid, a));
-        const float rx = tree8(r.x), ry = tree8(r.y), rz = tree8(r.z);
-        if (s == a && count > 0) {
-            float* part = B.cell_part + a * NC + base + node_offset(P, a);
-            part[0] = rx;
-            part[plane] = ry;
-            part[2 * plane] = rz;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const bm_v3 r = v3_mul(v, P.mass * w[a]);
+            vals[a][0] = r.x;
+            vals[a][1] = r.y;
+            vals[a][2] = r.z;
         }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) vals[a][0] = vals[a][1] = vals[a][2] = 0.0f;
+    }
+    float sum[3];
+    reduce_scatter8<3>(vals, sum);
+    base = __shfl_sync(kFull, base, threadIdx.x & ~7);
+    if (count > 0) {
+        float* part = B.cell_part + s * NC + base + node_offset(P, s);
+        const int plane = 8 * NC;
+        part[0] = sum[0];
+        part[plane] = sum[1];
+        part[2 * plane] = sum[2];
     }
 }
 
 // ---------------------------------------------------------- remap + couple
 
-// Remap sums of field f at node n from the cell partials (mixed cells recomputed).
-__device__ bm_v3 remap_node_sum(const bm_params& P, const bm_buffers& B, int n, int f) {
-    const int64_t N = P.n, NC = P.node_count, plane = 8 * NC;
+// Tree sum of the remap contributions of field f over cell c at corner a.
+__device__ __noinline__ bool remap_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, bm_v3* out) {
+    const int N = P.n;
+    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+    bm_v3 slot[8];
+    bool any = false;
+    for (int s = 0; s < 8; ++s) {
+        slot[s] = v3_zero();
+        if (s < count && field_of(B.fidx[b + s], a) == f) {
+            slot[s] = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
+            any = true;
+        }
+    }
+    if (!any) return false;
+    *out = v3(((slot[0].x + slot[1].x) + (slot[2].x + slot[3].x)) + ((slot[4].x + slot[5].x) + (slot[6].x + slot[7].x)),
+              ((slot[0].y + slot[1].y) + (slot[2].y + slot[3].y)) + ((slot[4].y + slot[5].y) + (slot[6].y + slot[7].y)),
+              ((slot[0].z + slot[1].z) + (slot[2].z + slot[3].z)) + ((slot[4].z + slot[5].z) + (slot[6].z + slot[7].z)));
+    return true;
+}
+
+// Remap sums of field f at node n from the cell partials.
+__device__ __forceinline__ bm_v3 remap_node_sum(const bm_params& P, const bm_buffers& B, int n, int f) {
+    const int NC = P.node_count, plane = 8 * NC;
     bm_v3 r = v3_zero();
-#pragma unroll 1
+#pragma unroll
     for (int a = 7; a >= 0; --a) {
-        const int c = cell_at(P, n, a);
-        if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
         const int flag = B.cell_field[a * NC + n];
         if (flag == f) {
             const float* part = B.cell_part + a * NC + n;
             r = v3_add(r, v3(part[0], part[plane], part[2 * plane]));
         } else if (flag == kMixed) {
-            const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-            bm_v3 slot[8];
-            bool any = false;
-            for (int s = 0; s < 8; ++s) {
-                slot[s] = v3_zero();
-                if (s < count && field_of(B.fidx[b + s], a) == f) {
-                    slot[s] = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
-                    any = true;
-                }
-            }
-            if (any)
-                r = v3_add(r, v3(((slot[0].x + slot[1].x) + (slot[2].x + slot[3].x)) + ((slot[4].x + slot[5].x) + (slot[6].x + slot[7].x)),
-                                 ((slot[0].y + slot[1].y) + (slot[2].y + slot[3].y)) + ((slot[4].y + slot[5].y) + (slot[6].y + slot[7].y)),
-                                 ((slot[0].z + slot[1].z) + (slot[2].z + slot[3].z)) + ((slot[4].z + slot[5].z) + (slot[6].z + slot[7].z))));
+            bm_v3 k;
+            if (remap_mixed(P, B, cell_at(P, n, a), a, f, &k)) r = v3_add(r, k);
         }
     }
     return r;
 }
 
-// Node pass of the MUSL re-scatter, then couple (material.py:155-193);
-// stores coupled / mass for the F update.
-__global__ void k_remap_couple(bm_params P, bm_buffers B) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.active_nodes) return;
-    const int n = B.active[t];
-    const int nf = B.nfield[n];
-    const int64_t S = (int64_t)P.fmax * P.node_count;
-    if (nf == 1) {
-        const bm_v3 r = remap_node_sum(P, B, n, 0);
-        const float m = B.grid_mass[n];
-        if (m <= 0.0f) {
-            st3(B.remap_v, S, n, v3_zero());
-            return;
-        }
-        const bm_v3 coupled = v3_add(r, v3_div(v3_zero(), m));
-        st3(B.remap_v, S, n, v3_div(coupled, m));
-        return;
-    }
-    for (int f = 0; f < nf; ++f) st3(B.remapped, S, (int64_t)f * P.node_count + n, remap_node_sum(P, B, n, f));
+__device__ __noinline__ void remap_multi_field(const bm_params& P, const bm_buffers& B, int n, int nf) {
+    const int S = P.fmax * P.node_count;
+    for (int f = 0; f < nf; ++f) st3(B.remapped, S, f * P.node_count + n, remap_node_sum(P, B, n, f));
     for (int f = 0; f < nf; ++f) {
-        const int64_t a = (int64_t)f * P.node_count + n;
+        const int a = f * P.node_count + n;
         const float ma = B.grid_mass[a];
         if (ma <= 0.0f) {
             st3(B.remap_v, S, a, v3_zero());
@@ -470,7 +492,7 @@ __global__ void k_remap_couple(bm_params P, bm_buffers B) {
         float total = 0.0f;
         bm_v3 ex = v3_zero();
         for (int g = 0; g < nf; ++g) {
-            const int64_t b = (int64_t)g * P.node_count + n;
+            const int b = g * P.node_count + n;
             const float mb = B.grid_mass[b];
             total = total + mb;
             if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
@@ -478,6 +500,28 @@ __global__ void k_remap_couple(bm_params P, bm_buffers B) {
         }
         st3(B.remap_v, S, a, v3_div(v3_add(sa, v3_div(ex, total)), ma));
     }
+}
+
+// Node pass of the MUSL re-scatter, then couple (material.py:155-193);
+// stores coupled / mass for the F update.
+__global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.active_nodes) return;
+    const int n = B.active[t];
+    const int nf = B.nfield[n];
+    const int S = P.fmax * P.node_count;
+    if (nf != 1) {
+        remap_multi_field(P, B, n, nf);
+        return;
+    }
+    const bm_v3 r = remap_node_sum(P, B, n, 0);
+    const float m = B.grid_mass[n];
+    if (m <= 0.0f) {
+        st3(B.remap_v, S, n, v3_zero());
+        return;
+    }
+    const bm_v3 coupled = v3_add(r, v3_div(v3_zero(), m));
+    st3(B.remap_v, S, n, v3_div(coupled, m));
 }
 
 // ---------------------------------------------------------- constitutive
@@ -510,7 +554,7 @@ __device__ bm_m33 corotated_svd(const bm_m33& U, bm_v3 s, const bm_m33& V, const
 
 // material.stress_at (material.py:94-112).
 __device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
-    const int64_t N = P.n;
+    const int N = P.n;
     const bm_m33 F = ld9(B.F, N, p);
     bm_m33 f = F, pinv = m33_identity();
     if (P.use_fp) {
@@ -530,7 +574,7 @@ __device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
 // material.plastic_at (material.py:404-431).
 __device__ bool plastic_at(const bm_params& P, const bm_buffers& B, int p, float yield_stress, bm_m33* U, bm_v3* s,
                            bm_m33* V) {
-    const int64_t N = P.n;
+    const int N = P.n;
     const bm_m33 F = ld9(B.F, N, p);
     bm_svd3(m33_mul(F, m33_inverse(ld9(B.Fp, N, p))), U, s, V);
     if (bm_minf(bm_minf(s->x, s->y), s->z) <= 0.0f) {
@@ -554,10 +598,10 @@ __device__ bool plastic_at(const bm_params& P, const bm_buffers& B, int p, float
 // material.maxwell_at (material.py:485-533).
 __device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const bm_m33& U, bm_v3 sigma,
                            const bm_m33& V, float relax) {
-    const int64_t N = P.n;
+    const int N = P.n;
     const bm_m33 f = m33_mul(m33_mul(U, m33_diag(sigma)), m33_transpose(V));
     double D[9];
-    for (int r = 0; r < 9; ++r) D[r] = B.viscous[(int64_t)r * N + p];
+    for (int r = 0; r < 9; ++r) D[r] = B.viscous[r * N + p];
     bm_m33 Df;
     for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) Df.m[r][c] = (float)D[3 * r + c];
@@ -587,7 +631,7 @@ __device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const
                 for (int k = 0; k < 3; ++k) prod = prod + dd[3 * r + k] * D[3 * k + c];
                 nd[3 * r + c] = (D[3 * r + c] + dd[3 * r + c]) + prod;
             }
-        for (int r = 0; r < 9; ++r) B.viscous[(int64_t)r * N + p] = nd[r];
+        for (int r = 0; r < 9; ++r) B.viscous[r * N + p] = nd[r];
     }
     const bm_m33 kirchhoff = m33_mul(m33_mul(Um, m33_diag(v3_mul(dev, 2.0f * P.mu_maxwell))), m33_transpose(Um));
     const float mu_eq = P.mu - P.mu_maxwell;
@@ -598,7 +642,7 @@ __device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const
 
 // material.maxwell_stress_at (material.py:536-566).
 __device__ void maxwell_stress_at(const bm_params& P, const bm_buffers& B, int p, float relax) {
-    const int64_t N = P.n;
+    const int N = P.n;
     bm_m33 U, V;
     bm_v3 sigma;
     if (P.yield_stress > 0.0f) {
@@ -671,7 +715,10 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
     const float band = 6.0f * P.spacing;
     for (int k = 0; k < P.tool_count; ++k) {
         const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
-        const bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, T.edge));
+        const bm_v3 d = v3_sub(xp, T.edge);
+        // cheap conservative band test on the knife axes (1 um beyond the exact bounds)
+        if (fabsf(v3_dot(d, T.ax)) > band + 1.0e-6f || fabsf(v3_dot(d, T.ay)) > P.half[1] + 1.0e-6f) continue;
+        const bm_v3 local = q_rotate_inv(T.rot, d);
         if (!(fabsf(local.x) <= band && fabsf(local.y) <= P.half[1])) continue;
         const float front = -local.z;
         const float advance = v3_dot(v3_sub(T.edge_vel, vp), T.down);
@@ -700,7 +747,9 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
     if (changed) {
         B.codes[p] = code;
         B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 1;
-        B.flags[BM_FLAG_PAIR_DIRTY] = 1;
+        // the pair lists of p and its neighbours are recomputed before the next pair pass
+        const int at = atomicAdd(&B.flags[BM_FLAG_CHANGED], 1);
+        if (at < P.n) B.changed[at] = p;
     }
 }
 
@@ -711,14 +760,14 @@ __global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int c
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
     if (p >= P.n) return;
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int N = P.n, S = P.fmax * P.node_count;
     if (do_update) {
         const int sid = B.stencil_id[p], base = B.base_node[p];
         const uint64_t fidx = B.fidx[p];
         bm_m33 rate = m33_zero();
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
-            const int64_t s = slot_of(P, base, fidx, a);
+            const int s = slot_of(P, base, fidx, a);
             if (B.grid_mass[s] > 0.0f) rate = m33_add(rate, m33_outer(ld3(B.remap_v, S, s), stencil_g(B, sid, a)));
         }
         st9(B.F, N, p, m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt)));
@@ -731,12 +780,12 @@ __global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int c
 __global__ void k_validate(bm_params P, bm_buffers B) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    const int64_t N = P.n;
+    const int N = P.n;
     const float d = m33_det(ld9(B.F, N, p));
     int bad = (d <= 0.0f || !bm_isfinitef(d)) ? 1 : 0;
     for (int i = 0; i < 3; ++i) {
-        if (!bm_isfinitef(B.x[(int64_t)i * N + p])) ++bad;
-        if (!bm_isfinitef(B.v[(int64_t)i * N + p])) ++bad;
+        if (!bm_isfinitef(B.x[i * N + p])) ++bad;
+        if (!bm_isfinitef(B.v[i * N + p])) ++bad;
     }
     if (bad) atomicAdd(&B.errors[1], bad);
 }
@@ -746,7 +795,7 @@ __global__ void k_validate(bm_params P, bm_buffers B) {
 __global__ void k_viscous_stress(bm_params P, bm_buffers B, float* __restrict__ out) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int N = P.n, S = P.fmax * P.node_count;
     const int sid = B.stencil_id[p], base = B.base_node[p];
     const uint64_t fidx = B.fidx[p];
     bm_m33 rate = m33_zero();
@@ -763,10 +812,10 @@ __global__ void k_viscous_gather(bm_params P, bm_buffers B, const float* __restr
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     const int nf = B.nfield[n];
-    const int64_t N = P.n, S = (int64_t)P.fmax * P.node_count;
+    const int N = P.n, S = P.fmax * P.node_count;
     const float scale = -P.dt * P.volume;
     for (int f = 0; f < nf; ++f) {
-        const int64_t slot = (int64_t)f * P.node_count + n;
+        const int slot = f * P.node_count + n;
         bm_v3 J = ld3(B.grid_impulse, S, slot);
         for_contributions(P, B, n, [&](int p, int a) {
             if (field_of(B.fidx[p], a) != f) return;
@@ -785,9 +834,9 @@ __global__ void k_couple_slots(bm_params P, bm_buffers B, const float* __restric
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     const int nf = B.nfield[n];
-    const int64_t S = (int64_t)P.fmax * P.node_count;
+    const int S = P.fmax * P.node_count;
     for (int f = 0; f < nf; ++f) {
-        const int64_t a = (int64_t)f * P.node_count + n;
+        const int a = f * P.node_count + n;
         const float ma = B.grid_mass[a];
         if (ma <= 0.0f) continue;
         const bm_v3 sa = ld3(state, S, a);
@@ -795,7 +844,7 @@ __global__ void k_couple_slots(bm_params P, bm_buffers B, const float* __restric
         float total = 0.0f;
         bm_v3 ex = v3_zero();
         for (int g = 0; g < nf; ++g) {
-            const int64_t b = (int64_t)g * P.node_count + n;
+            const int b = g * P.node_count + n;
             const float mb = B.grid_mass[b];
             total = total + mb;
             if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
@@ -810,9 +859,9 @@ __global__ void k_grid_vel(bm_params P, bm_buffers B, const float* __restrict__ 
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     const int nf = B.nfield[n];
-    const int64_t S = (int64_t)P.fmax * P.node_count;
+    const int S = P.fmax * P.node_count;
     for (int f = 0; f < nf; ++f) {
-        const int64_t s = (int64_t)f * P.node_count + n;
+        const int s = f * P.node_count + n;
         const float m = B.grid_mass[s];
         if (m > 0.0f) {
             const bm_v3 pm = ld3(momentum, S, s);
@@ -836,10 +885,10 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
-    const int64_t S = (int64_t)P.fmax * P.node_count;
+    const int S = P.fmax * P.node_count;
     if (P.viscous) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
-        k_p2g_cells<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
+        k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, 1);
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.grid_impulse);
@@ -850,14 +899,14 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.remap_v);
         (void)S;
     } else {
-        k_p2g_cells<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
+        k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, write_sums);
     }
 }
 
 void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
-    k_g2p<<<grid_for(8 * (int64_t)P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(
+    k_g2p<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(
         P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
 }
 

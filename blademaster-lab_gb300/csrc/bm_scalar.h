@@ -358,8 +358,10 @@ BM_HD bm_qd qd_from_axis_angle(bm_v3d axis, double angle) {
 /* --------------------------------------------------------- 3x3 polar / SVD */
 
 /* Rotation factor of the polar decomposition of a (det a > 0 assumed).
- * Newton's iteration X <- (X + X^-T)/2 from X = a, stopped when the update
- * changes X by at most 4 ulp of 1 in max norm, or after 16 iterations. */
+ * Newton's iteration X <- (X + X^-T)/2 from X = a converges quadratically:
+ * an update of size d leaves an error of about d^2 / 2, so the iteration
+ * stops after an update below 1e-4 (remaining error < 1e-8, below float
+ * resolution), or after 16 iterations. */
 BM_HD bm_m33 bm_polar3(bm_m33 a) {
     bm_m33 x = a, y;
     int it, i, j;
@@ -372,7 +374,7 @@ BM_HD bm_m33 bm_polar3(bm_m33 a) {
                 change = bm_maxf(change, fabsf(y.m[i][j] - x.m[i][j]));
             }
         x = y;
-        if (!(change > 4.8e-7f)) break;
+        if (!(change > 1.0e-4f)) break;
     }
     return x;
 }

@@ -52,7 +52,18 @@ __device__ void write_mirror(const bm_params& P, const bm_buffers& B, int k) {
     f[21] = edge_vel.x;
     f[22] = edge_vel.y;
     f[23] = edge_vel.z;
-    f[24] = 0.0f;
+    const bm_v3 ax = q_rotate(q, v3(1.0f, 0.0f, 0.0f)), ay = q_rotate(q, v3(0.0f, 1.0f, 0.0f)),
+                az = q_rotate(q, v3(0.0f, 0.0f, 1.0f));
+    f[24] = ax.x;
+    f[25] = ax.y;
+    f[26] = ax.z;
+    f[27] = ay.x;
+    f[28] = ay.y;
+    f[29] = ay.z;
+    f[30] = az.x;
+    f[31] = az.y;
+    f[32] = az.z;
+    f[33] = f[34] = f[35] = 0.0f;
 }
 
 // tool.vertex (tool.py:118-138).

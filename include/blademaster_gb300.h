@@ -44,8 +44,8 @@ extern "C" {
 
 #define BM_MAX_TOOLS 16
 /* Float32 knife record: pos 3, vel 3, rot 4, omega 3, |vel| 1, |omega| * blade radius 1,
- * edge centre 3, cutting direction 3, edge velocity 3, padding 1. */
-#define BM_TOOL_F_WORDS 25
+ * edge centre 3, cutting direction 3, edge velocity 3, knife axes 9, padding 3. */
+#define BM_TOOL_F_WORDS 36
 #define BM_PAIR_LANES 64
 
 /* Scalars of one solver: Config (solver.py:12-149) plus the derived
@@ -143,6 +143,10 @@ typedef struct bm_buffers {
     float* pair_history; /* [2][pair_capacity][3] */
     int32_t* pair_used;  /* [2][pair_capacity] */
     int32_t* pair_count; /* [2] */
+    int32_t* changed;    /* [n] particles whose cut code changed since the last list update */
+    int32_t* relist;     /* [n] 1 while a particle's partner list awaits recomputation */
+    int32_t* relist_list;/* [n] those particles */
+    int32_t* listed;     /* [n] 1 if the particle is in candidates */
     /* tool and scalar state */
     double* tool;        /* [tools][13]: pos 3, vel 3, rot xyzw 4, omega 3 */
     float* tool_f;       /* [tools][BM_TOOL_F_WORDS] float32 mirror read by particle kernels */
@@ -176,7 +180,9 @@ typedef struct bm_buffers {
 #define BM_FLAG_CANDIDATES 4     /* number of pair candidates */
 #define BM_FLAG_EMBEDDED 5       /* count_embedded result */
 #define BM_FLAG_SLOTS 6          /* registered slots */
-#define BM_FLAG_WORDS 8
+#define BM_FLAG_CHANGED 7        /* entries of buffers.changed */
+#define BM_FLAG_RELIST 8         /* entries of buffers.relist_list */
+#define BM_FLAG_WORDS 12
 
 typedef struct bm_solver bm_solver;
 typedef struct bm_graph bm_graph;
