@@ -41,6 +41,10 @@ __device__ __forceinline__ void for_contributions(const bm_params& P, const bm_b
 // contributors in ascending order (material.register, material.py:50-66).
 __device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n);
 
+__global__ void k_register_begin(bm_buffers B, int force) {
+    if (force || B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0) B.flags[BM_FLAG_MULTI] = 0;
+}
+
 __global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
     if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P.active_nodes; t += gridDim.x * blockDim.x)
@@ -77,6 +81,7 @@ __device__ void register_node(const bm_params& P, const bm_buffers& B, const int
         have_prev = true;
     }
     B.nfield[n] = nf;
+    if (nf > 1) B.multi_nodes[atomicAdd(&B.flags[BM_FLAG_MULTI], 1)] = n;
 }
 
 // Particle pass: the field index of the particle's code at each stencil node.
@@ -160,6 +165,75 @@ __device__ __forceinline__ int cell_at(const bm_params& P, int n, int a) {
     return (ci * P.cell_dims[1] + cj) * P.cell_dims[2] + ck;
 }
 
+// A cell group (8 lanes, mask gmask) with at least one mixed corner: for every
+// mixed corner, the tree sums of each field present (other lanes +0) are
+// appended to mixed_part as one run, ascending field; mixed_run[node][a]
+// records it (-1 when the buffer is full: the node pass then recomputes).
+template <int V>
+__device__ void emit_mixed_runs(const bm_params& P, const bm_buffers& B, const float (&vals)[8][V], uint64_t fidx,
+                                bool present, int base, unsigned gmask) {
+    const int s = threadIdx.x & 7;
+    const int lead = (threadIdx.x & 31) & ~7;
+    for (int a = 0; a < 8; ++a) {
+        const int f = present ? field_of(fidx, a) : 255;
+        int lo = f, hi = present ? f : -1;
+        for (int d = 1; d < 8; d <<= 1) {
+            lo = min(lo, __shfl_xor_sync(gmask, lo, d));
+            hi = max(hi, __shfl_xor_sync(gmask, hi, d));
+        }
+        if (lo == hi) continue;
+        int runs = 0;
+        for (int cur = lo; cur != 255;) {
+            ++runs;
+            int next = f > cur ? f : 255;
+            for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
+            cur = next;
+        }
+        int at = 0;
+        if (s == 0) at = atomicAdd(&B.flags[BM_FLAG_MIXED], runs);
+        at = __shfl_sync(gmask, at, lead);
+        const int node = base + node_offset(P, a);
+        const bool fits = at + runs <= P.mixed_capacity;
+        if (s == 0) B.mixed_run[node * 8 + a] = fits ? (at << 4) | runs : -1;
+        if (!fits) continue;
+        int k = 0;
+        for (int cur = lo; cur != 255; ++k) {
+            float out[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                float x = f == cur ? vals[a][v] : 0.0f;
+                x = x + __shfl_xor_sync(gmask, x, 1);
+                x = x + __shfl_xor_sync(gmask, x, 2);
+                x = x + __shfl_xor_sync(gmask, x, 4);
+                out[v] = x;
+            }
+            if (s == 0) {
+                float* e = B.mixed_part + 8 * (at + k);
+#pragma unroll
+                for (int v = 0; v < V; ++v) e[v] = out[v];
+                e[7] = __int_as_float(cur);
+            }
+            int next = f > cur ? f : 255;
+            for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
+            cur = next;
+        }
+    }
+}
+
+// The run entry of field f at mixed corner (n, a); false if f has no
+// particle there; *missing when the run was not stored.
+__device__ __forceinline__ const float* mixed_entry(const bm_buffers& B, int n, int a, int f, bool* missing) {
+    const int run = B.mixed_run[n * 8 + a];
+    *missing = run < 0;
+    if (run < 0) return nullptr;
+    const int start = run >> 4, len = run & 15;
+    for (int k = 0; k < len; ++k) {
+        const float* e = B.mixed_part + 8 * (start + k);
+        if (__float_as_int(e[7]) == f) return e;
+    }
+    return nullptr;
+}
+
 struct P2GContrib {
     float m;
     bm_v3 mom, J;
@@ -240,8 +314,10 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
         float* part = B.cell_part + s * NC + node;
 #pragma unroll
         for (int v = 0; v < 7; ++v) part[v * plane] = sum[v];
-        B.cell_field[s * NC + node] = (uint8_t)(lo == hi ? lo : kMixed);
+        B.cell_field[node * 8 + s] = (uint8_t)(lo == hi ? lo : kMixed);
     }
+    const unsigned mixed = __ballot_sync(kFull, count > 0 && lo != hi);
+    if ((mixed >> (group & 31)) & 0xffu) emit_mixed_runs<7>(P, B, vals, fidx, present, base, 0xffu << (group & 31));
 }
 
 // The tree sum of field f over the particles of cell c at corner a (a cell
@@ -279,86 +355,72 @@ __device__ __noinline__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, 
     return true;
 }
 
-// Node pass of p2g: field sums over the adjacent cells' partials, in
-// ascending cell index (a = 7 .. 0).
-__device__ __forceinline__ NodeSums p2g_node_sums(const bm_params& P, const bm_buffers& B, int n, int f) {
+// Node pass of p2g for field f: the adjacent cells' partials in ascending
+// cell index (a = 7 .. 0); mixed corners from their runs (or recomputed).
+__device__ NodeSums p2g_node_sums_multi(const bm_params& P, const bm_buffers& B, int n, int f) {
     const int NC = P.node_count, plane = 8 * NC;
     NodeSums r;
     r.m = 0.0f;
     r.mom = v3_zero();
     r.J = v3_zero();
-#pragma unroll
     for (int a = 7; a >= 0; --a) {
-        const int flag = B.cell_field[a * NC + n];
+        const int flag = B.cell_field[n * 8 + a];
         if (flag == f) {
             const float* part = B.cell_part + a * NC + n;
             r.m = r.m + part[0];
             r.mom = v3_add(r.mom, v3(part[plane], part[2 * plane], part[3 * plane]));
             r.J = v3_add(r.J, v3(part[4 * plane], part[5 * plane], part[6 * plane]));
         } else if (flag == kMixed) {
-            P2GContrib k;
-            if (p2g_mixed(P, B, cell_at(P, n, a), a, f, &k)) {
-                r.m = r.m + k.m;
-                r.mom = v3_add(r.mom, k.mom);
-                r.J = v3_add(r.J, k.J);
+            bool missing;
+            const float* e = mixed_entry(B, n, a, f, &missing);
+            if (e) {
+                r.m = r.m + e[0];
+                r.mom = v3_add(r.mom, v3(e[1], e[2], e[3]));
+                r.J = v3_add(r.J, v3(e[4], e[5], e[6]));
+            } else if (missing) {
+                P2GContrib k;
+                if (p2g_mixed(P, B, cell_at(P, n, a), a, f, &k)) {
+                    r.m = r.m + k.m;
+                    r.mom = v3_add(r.mom, k.mom);
+                    r.J = v3_add(r.J, k.J);
+                }
             }
         }
     }
     return r;
 }
 
-// Exchange of a node with several fields (material.py:252-284).
-__device__ __noinline__ void p2g_multi_field(const bm_params& P, const bm_buffers& B, int n, int nf) {
-    const int S = P.fmax * P.node_count;
-    for (int f = 0; f < nf; ++f) {
-        const NodeSums s = p2g_node_sums(P, B, n, f);
-        const int slot = f * P.node_count + n;
-        B.grid_mass[slot] = s.m;
-        st3(B.momentum, S, slot, s.mom);
-        st3(B.grid_impulse, S, slot, s.J);
-    }
-    for (int f = 0; f < nf; ++f) {
-        const int a = f * P.node_count + n;
-        const float ma = B.grid_mass[a];
-        if (ma <= 0.0f) {
-            st3(B.old_v, S, a, v3_zero());
-            st3(B.new_v, S, a, v3_zero());
-            continue;
-        }
-        const bm_v3 pa = ld3(B.momentum, S, a), ja = ld3(B.grid_impulse, S, a);
-        const uint64_t oa = B.fones[a], ta = B.ftwos[a];
-        float total = 0.0f;
-        bm_v3 dm = v3_zero(), di = v3_zero();
-        for (int g = 0; g < nf; ++g) {
-            const int b = g * P.node_count + n;
-            const float mb = B.grid_mass[b];
-            total = total + mb;
-            if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b])) {
-                dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, b), ma), v3_mul(pa, mb)));
-                di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, b), ma), v3_mul(ja, mb)));
-            }
-        }
-        const bm_v3 pm = v3_add(pa, v3_div(dm, total));
-        const bm_v3 jm = v3_add(ja, v3_div(di, total));
-        st3(B.old_v, S, a, v3_div(pm, ma));
-        st3(B.new_v, S, a, v3_div(v3_add(pm, jm), ma));
-    }
-}
-
-// p2g node sums + couple_and_velocity (material.py:127-152, 252-284), one
-// thread per active node; also clears the topology flag consumed by registration.
+// p2g node sums + couple_and_velocity (material.py:127-152, 252-284) for the
+// single-field nodes, one thread per active node (a single-field node has no
+// mixed corner: every corner is field 0 or has no cell).  Also clears the
+// topology flag consumed by registration and the mixed-run counter.
 __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
+    if (t == 0) {
+        B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
+        B.flags[BM_FLAG_MIXED] = 0;  // the re-scatter's runs start over (p2g runs are read by k_p2g_multi only)
+    }
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
-    const int nf = B.nfield[n];
-    const int S = P.fmax * P.node_count;
-    if (nf != 1) {
-        p2g_multi_field(P, B, n, nf);
-        return;
+    if (B.nfield[n] != 1) return;
+    const int NC = P.node_count, S = P.fmax * NC, plane = 8 * NC;
+    const uint64_t flags = *reinterpret_cast<const uint64_t*>(B.cell_field + 8 * n);
+    float part[8][7];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int v = 0; v < 7; ++v) part[a][v] = B.cell_part[v * plane + a * NC + n];
+    NodeSums s;
+    s.m = 0.0f;
+    s.mom = v3_zero();
+    s.J = v3_zero();
+#pragma unroll
+    for (int a = 7; a >= 0; --a) {
+        if (((flags >> (8 * a)) & 0xffu) != 0u) continue;  // no cell at this corner
+        s.m = s.m + part[a][0];
+        s.mom = v3_add(s.mom, v3(part[a][1], part[a][2], part[a][3]));
+        s.J = v3_add(s.J, v3(part[a][4], part[a][5], part[a][6]));
     }
-    const NodeSums s = p2g_node_sums(P, B, n, 0);
     B.grid_mass[n] = s.m;
     if (write_sums) {
         st3(B.momentum, S, n, s.mom);
@@ -373,6 +435,50 @@ __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int
     const bm_v3 jm = v3_add(s.J, v3_div(v3_zero(), s.m));
     st3(B.old_v, S, n, v3_div(pm, s.m));
     st3(B.new_v, S, n, v3_div(v3_add(pm, jm), s.m));
+}
+
+// The nodes with several fields (listed at registration): field sums and the
+// exchange of couple_and_velocity (material.py:252-284).
+__global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
+    const int count = B.flags[BM_FLAG_MULTI];
+    const int S = P.fmax * P.node_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int n = B.multi_nodes[t];
+        const int nf = B.nfield[n];
+        for (int f = 0; f < nf; ++f) {
+            const NodeSums s = p2g_node_sums_multi(P, B, n, f);
+            const int slot = f * P.node_count + n;
+            B.grid_mass[slot] = s.m;
+            st3(B.momentum, S, slot, s.mom);
+            st3(B.grid_impulse, S, slot, s.J);
+        }
+        for (int f = 0; f < nf; ++f) {
+            const int a = f * P.node_count + n;
+            const float ma = B.grid_mass[a];
+            if (ma <= 0.0f) {
+                st3(B.old_v, S, a, v3_zero());
+                st3(B.new_v, S, a, v3_zero());
+                continue;
+            }
+            const bm_v3 pa = ld3(B.momentum, S, a), ja = ld3(B.grid_impulse, S, a);
+            const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+            float total = 0.0f;
+            bm_v3 dm = v3_zero(), di = v3_zero();
+            for (int g = 0; g < nf; ++g) {
+                const int b = g * P.node_count + n;
+                const float mb = B.grid_mass[b];
+                total = total + mb;
+                if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b])) {
+                    dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, b), ma), v3_mul(pa, mb)));
+                    di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, b), ma), v3_mul(ja, mb)));
+                }
+            }
+            const bm_v3 pm = v3_add(pa, v3_div(dm, total));
+            const bm_v3 jm = v3_add(ja, v3_div(di, total));
+            st3(B.old_v, S, a, v3_div(pm, ma));
+            st3(B.new_v, S, a, v3_div(v3_add(pm, jm), ma));
+        }
+    }
 }
 
 // ------------------------------------------------------------------- G2P
@@ -427,13 +533,22 @@ __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float ha
     }
     float sum[3];
     reduce_scatter8<3>(vals, sum);
-    base = __shfl_sync(kFull, base, threadIdx.x & ~7);
+    const int group = threadIdx.x & ~7;
+    base = __shfl_sync(kFull, base, group);
+    bool mixed_corner = false;
     if (count > 0) {
-        float* part = B.cell_part + s * NC + base + node_offset(P, s);
+        const int node = base + node_offset(P, s);
+        float* part = B.cell_part + s * NC + node;
         const int plane = 8 * NC;
         part[0] = sum[0];
         part[plane] = sum[1];
         part[2 * plane] = sum[2];
+        mixed_corner = B.cell_field[node * 8 + s] == kMixed;
+    }
+    const unsigned mixed = __ballot_sync(kFull, mixed_corner);
+    if ((mixed >> (group & 31)) & 0xffu) {
+        uint64_t fidx = present ? B.fidx[p] : 0u;
+        emit_mixed_runs<3>(P, B, vals, fidx, present, base, 0xffu << (group & 31));
     }
 }
 
@@ -459,62 +574,50 @@ __device__ __noinline__ bool remap_mixed(const bm_params& P, const bm_buffers& B
     return true;
 }
 
-// Remap sums of field f at node n from the cell partials.
-__device__ __forceinline__ bm_v3 remap_node_sum(const bm_params& P, const bm_buffers& B, int n, int f) {
+// Remap sums of field f at node n (multi-field nodes): partials, runs, or recomputed.
+__device__ bm_v3 remap_node_sum_multi(const bm_params& P, const bm_buffers& B, int n, int f) {
     const int NC = P.node_count, plane = 8 * NC;
     bm_v3 r = v3_zero();
-#pragma unroll
     for (int a = 7; a >= 0; --a) {
-        const int flag = B.cell_field[a * NC + n];
+        const int flag = B.cell_field[n * 8 + a];
         if (flag == f) {
             const float* part = B.cell_part + a * NC + n;
             r = v3_add(r, v3(part[0], part[plane], part[2 * plane]));
         } else if (flag == kMixed) {
-            bm_v3 k;
-            if (remap_mixed(P, B, cell_at(P, n, a), a, f, &k)) r = v3_add(r, k);
+            bool missing;
+            const float* e = mixed_entry(B, n, a, f, &missing);
+            if (e) {
+                r = v3_add(r, v3(e[0], e[1], e[2]));
+            } else if (missing) {
+                bm_v3 k;
+                if (remap_mixed(P, B, cell_at(P, n, a), a, f, &k)) r = v3_add(r, k);
+            }
         }
     }
     return r;
 }
 
-__device__ __noinline__ void remap_multi_field(const bm_params& P, const bm_buffers& B, int n, int nf) {
-    const int S = P.fmax * P.node_count;
-    for (int f = 0; f < nf; ++f) st3(B.remapped, S, f * P.node_count + n, remap_node_sum(P, B, n, f));
-    for (int f = 0; f < nf; ++f) {
-        const int a = f * P.node_count + n;
-        const float ma = B.grid_mass[a];
-        if (ma <= 0.0f) {
-            st3(B.remap_v, S, a, v3_zero());
-            continue;
-        }
-        const bm_v3 sa = ld3(B.remapped, S, a);
-        const uint64_t oa = B.fones[a], ta = B.ftwos[a];
-        float total = 0.0f;
-        bm_v3 ex = v3_zero();
-        for (int g = 0; g < nf; ++g) {
-            const int b = g * P.node_count + n;
-            const float mb = B.grid_mass[b];
-            total = total + mb;
-            if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
-                ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, b), ma), v3_mul(sa, mb)));
-        }
-        st3(B.remap_v, S, a, v3_div(v3_add(sa, v3_div(ex, total)), ma));
-    }
-}
-
-// Node pass of the MUSL re-scatter, then couple (material.py:155-193);
-// stores coupled / mass for the F update.
+// Node pass of the MUSL re-scatter, then couple (material.py:155-193) for the
+// single-field nodes; stores coupled / mass for the F update.
 __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // the next p2g's runs start over
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
-    const int nf = B.nfield[n];
-    const int S = P.fmax * P.node_count;
-    if (nf != 1) {
-        remap_multi_field(P, B, n, nf);
-        return;
+    if (B.nfield[n] != 1) return;
+    const int NC = P.node_count, S = P.fmax * NC, plane = 8 * NC;
+    const uint64_t flags = *reinterpret_cast<const uint64_t*>(B.cell_field + 8 * n);
+    float part[8][3];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int v = 0; v < 3; ++v) part[a][v] = B.cell_part[v * plane + a * NC + n];
+    bm_v3 r = v3_zero();
+#pragma unroll
+    for (int a = 7; a >= 0; --a) {
+        if (((flags >> (8 * a)) & 0xffu) != 0u) continue;
+        r = v3_add(r, v3(part[a][0], part[a][1], part[a][2]));
     }
-    const bm_v3 r = remap_node_sum(P, B, n, 0);
     const float m = B.grid_mass[n];
     if (m <= 0.0f) {
         st3(B.remap_v, S, n, v3_zero());
@@ -522,6 +625,36 @@ __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B)
     }
     const bm_v3 coupled = v3_add(r, v3_div(v3_zero(), m));
     st3(B.remap_v, S, n, v3_div(coupled, m));
+}
+
+__global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) {
+    const int count = B.flags[BM_FLAG_MULTI];
+    const int S = P.fmax * P.node_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int n = B.multi_nodes[t];
+        const int nf = B.nfield[n];
+        for (int f = 0; f < nf; ++f) st3(B.remapped, S, f * P.node_count + n, remap_node_sum_multi(P, B, n, f));
+        for (int f = 0; f < nf; ++f) {
+            const int a = f * P.node_count + n;
+            const float ma = B.grid_mass[a];
+            if (ma <= 0.0f) {
+                st3(B.remap_v, S, a, v3_zero());
+                continue;
+            }
+            const bm_v3 sa = ld3(B.remapped, S, a);
+            const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+            float total = 0.0f;
+            bm_v3 ex = v3_zero();
+            for (int g = 0; g < nf; ++g) {
+                const int b = g * P.node_count + n;
+                const float mb = B.grid_mass[b];
+                total = total + mb;
+                if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
+                    ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, b), ma), v3_mul(sa, mb)));
+            }
+            st3(B.remap_v, S, a, v3_div(v3_add(sa, v3_div(ex, total)), ma));
+        }
+    }
 }
 
 // ---------------------------------------------------------- constitutive
@@ -878,6 +1011,7 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
     const unsigned wide = 8 * 152;  // grid-stride: cheap to launch when the gate is off
     const unsigned gn = grid_for(P.active_nodes) < wide ? grid_for(P.active_nodes) : wide;
     const unsigned gp = grid_for(P.n) < wide ? grid_for(P.n) : wide;
+    k_register_begin<<<1, 1, 0, st>>>(s->B, force);
     k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes, force);
     k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes, force);
 }
@@ -890,6 +1024,7 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
         k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, 1);
+        k_p2g_multi<<<2 * 152, kBlock, 0, st>>>(P, B);
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.grid_impulse);
         k_viscous_stress<<<grid_for(P.n), kBlock, 0, st>>>(P, B, s->viscous_scratch);
@@ -901,6 +1036,7 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     } else {
         k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
         k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, write_sums);
+        k_p2g_multi<<<2 * 152, kBlock, 0, st>>>(P, B);
     }
 }
 
@@ -913,6 +1049,7 @@ void launch_g2p(const bm_solver* s, cudaStream_t st) {
 void launch_remap(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
     k_remap_couple<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B);
+    k_remap_multi<<<2 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
 void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,

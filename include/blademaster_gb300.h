@@ -64,6 +64,8 @@ typedef struct bm_params {
     int32_t pair_capacity;     /* friction-history hash table size (power of two) */
     int32_t bucket_mask;       /* pair search buckets - 1 (power of two) */
     int32_t candidate_capacity;
+    int32_t mixed_capacity;    /* entries of buffers.mixed_part */
+    int32_t pad_sizes;
     /* mode flags */
     int32_t tool_model;        /* -1 external, 0 guided, 1 free/servo (solver.py:571-576) */
     int32_t external_tool;
@@ -128,7 +130,10 @@ typedef struct bm_buffers {
     float* remapped;     /* [3][fmax * node_count] remapped momentum (multi-field nodes) */
     float* remap_v;      /* [3][fmax * node_count] coupled remapped momentum / mass */
     float* cell_part;    /* [7][8][node_count] cell-corner partial sums: from the cell whose corner a is node n */
-    uint8_t* cell_field; /* [8][node_count] field index of a uniform cell corner, 255 if its particles differ */
+    uint8_t* cell_field; /* [node_count][8] field index of a uniform cell corner, 255 mixed, 254 no cell */
+    int32_t* mixed_run;  /* [node_count][8] start << 4 | length of a mixed corner's per-field partials, -1 none */
+    float* mixed_part;   /* [mixed_capacity][8] per-field partials of mixed corners (7 sums, field as float) */
+    int32_t* multi_nodes;/* [active_nodes] nodes with more than one field */
     /* pair contact */
     float* built_x;      /* [3][n] */
     int64_t* built_codes;/* [n] */
@@ -182,6 +187,8 @@ typedef struct bm_buffers {
 #define BM_FLAG_SLOTS 6          /* registered slots */
 #define BM_FLAG_CHANGED 7        /* entries of buffers.changed */
 #define BM_FLAG_RELIST 8         /* entries of buffers.relist_list */
+#define BM_FLAG_MULTI 9          /* entries of buffers.multi_nodes */
+#define BM_FLAG_MIXED 10         /* entries of buffers.mixed_part in use */
 #define BM_FLAG_WORDS 12
 
 typedef struct bm_solver bm_solver;
