@@ -256,6 +256,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    counters_before = s._t["flags"].cpu().numpy().copy()
     start.record()
     run(args.steps)
     end.record()
@@ -272,6 +273,13 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     slots = int(s._t["nfield"].sum().item())
+    counters_after = s._t["flags"].cpu().numpy()
+    events = {
+        "pair_list_builds": int(counters_after[_native.FLAG["PAIR_BUILDS"]] - counters_before[_native.FLAG["PAIR_BUILDS"]]),
+        "registrations": int(counters_after[_native.FLAG["REGISTRATIONS"]] - counters_before[_native.FLAG["REGISTRATIONS"]]),
+        "multi_field_nodes": int(counters_after[_native.FLAG["MULTI"]]),
+        "mixed_cells": int(counters_after[_native.FLAG["MIXED_CELLS"]]),
+    }
     value = world * s.n * args.steps / (ms / 1e3)
 
     # per-stage device time (CUDA events around each stage, eager launches)
@@ -347,6 +355,7 @@ def main():
             "d2h_bytes_per_step": int(pinned_state.numel() * 8),
         },
         "device_errors": errors,
+        "timed_region_events": events,
     }
     launches_per_substep = 19
     line["gpu_launches"] = launches_per_substep * args.steps

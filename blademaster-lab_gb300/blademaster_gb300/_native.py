@@ -131,7 +131,11 @@ def header_constant(name):
 PAIR_LANES = int(header_constant("BM_PAIR_LANES"))
 MAX_TOOLS = int(header_constant("BM_MAX_TOOLS"))
 TOOL_F_WORDS = int(header_constant("BM_TOOL_F_WORDS"))
-FLAG = {k: int(header_constant("BM_FLAG_" + k)) for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "WORDS")}
+FLAG = {
+    k: int(header_constant("BM_FLAG_" + k))
+    for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "CHANGED",
+              "RELIST", "MULTI", "MIXED", "MIXED_CELLS", "REGISTRATIONS", "WORDS")
+}
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
 STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate"]
 ACC_WORDS = 2 * (6 * MAX_TOOLS + 4)

@@ -257,6 +257,7 @@ class Solver:
         self.mixed_capacity = 8 * self.node_count
         T["mixed_part"] = zeros(self.mixed_capacity, 8)
         T["multi_nodes"] = zeros(len(active), dtype=i32)
+        T["mixed_cells"] = zeros(int(np.prod(cells)), dtype=i32)
         T["hist_mask"] = t.full((n,), -1, dtype=t.int16, device=dev)
         T["built_x"] = zeros(3, n)
         T["built_codes"] = zeros(n, dtype=i64)
@@ -267,6 +268,9 @@ class Solver:
         T["bucket_items"] = zeros(n, dtype=i32)
         T["bucket_fill"] = zeros(self.buckets, dtype=i32)
         T["particle_bucket"] = zeros(n, dtype=i32)
+        T["particle_key"] = zeros(n, dtype=i64)
+        T["bucket_key"] = zeros(n, dtype=i64)
+        T["bucket_pos"] = zeros(n, 4)
         T["pair_keys"] = t.full((2, self.pair_capacity), -1, dtype=i64, device=dev)
         T["pair_history"] = zeros(2, self.pair_capacity, 3)
         T["pair_used"] = zeros(2, self.pair_capacity, dtype=i32)

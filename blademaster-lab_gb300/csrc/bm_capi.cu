@@ -160,7 +160,8 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
                               buffers->targets, buffers->rotations, buffers->packed, buffers->result,
                               buffers->scratch, buffers->cell_part, buffers->cell_field, buffers->hist_mask,
                               buffers->changed, buffers->relist, buffers->relist_list, buffers->listed,
-                              buffers->mixed_run, buffers->mixed_part, buffers->multi_nodes};
+                              buffers->mixed_run, buffers->mixed_part, buffers->multi_nodes, buffers->mixed_cells,
+                              buffers->particle_key, buffers->bucket_key, buffers->bucket_pos};
     for (const void* ptr : required)
         if (!ptr) return fail(BM_ERR_ARGUMENT, "a required buffer is null");
     if (P.maxwell && !buffers->viscous) return fail(BM_ERR_ARGUMENT, "maxwell requires the viscous buffer");

@@ -397,6 +397,11 @@ __device__ bool pair_impulse(const bm_params& P, const bm_buffers& B, int p, int
 }
 
 __device__ __forceinline__ int cell_coord(float x, float size) { return (int)floorf(x / size); }
+// Cell coordinates packed 21 bits each (cells more than 2^20 apart may alias,
+// which only adds candidates that the distance test rejects).
+__device__ __forceinline__ int64_t cell_key(int cx, int cy, int cz) {
+    return (int64_t)((((uint64_t)cx & 0x1FFFFFu) << 42) | (((uint64_t)cy & 0x1FFFFFu) << 21) | ((uint64_t)cz & 0x1FFFFFu));
+}
 // contact.list_bucket (contact.py:743-745).
 __device__ __forceinline__ int list_bucket(int cx, int cy, int cz, int mask) {
     return (int)((((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u)) &
@@ -454,8 +459,10 @@ __global__ void k_bin_count(bm_params P, bm_buffers B, const float* reach_in, co
     const float reach = *reach_in;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) {
         const bm_v3 x = ld3(B.x, N, p);
-        const int b = list_bucket(cell_coord(x.x, reach), cell_coord(x.y, reach), cell_coord(x.z, reach), P.bucket_mask);
+        const int cx = cell_coord(x.x, reach), cy = cell_coord(x.y, reach), cz = cell_coord(x.z, reach);
+        const int b = list_bucket(cx, cy, cz, P.bucket_mask);
         B.particle_bucket[p] = b;
+        B.particle_key[p] = cell_key(cx, cy, cz);
         atomicAdd(&B.bucket_fill[b], 1);
     }
 }
@@ -518,6 +525,9 @@ __global__ void k_bin_scatter(bm_params P, bm_buffers B, const int32_t* gate_fla
         const int b = B.particle_bucket[p];
         const int at = B.bucket_start[b] + atomicSub(&B.bucket_fill[b], 1) - 1;
         B.bucket_items[at] = p;
+        B.bucket_key[at] = B.particle_key[p];
+        const bm_v3 x = ld3(B.x, P.n, p);
+        reinterpret_cast<float4*>(B.bucket_pos)[at] = make_float4(x.x, x.y, x.z, 0.0f);
     }
 }
 
@@ -540,18 +550,21 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
     B.built_codes[p] = cp;
     const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
     int32_t* list = B.partners + (int64_t)p * BM_PAIR_LANES;
+    const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
     int count = 0;
     for (int i = 0; i < 27; ++i) {
         const int cx = hx + i % 3 - 1, cy = hy + (i / 3) % 3 - 1, cz = hz + i / 9 - 1;
         const int b = list_bucket(cx, cy, cz, P.bucket_mask);
+        const int64_t key = cell_key(cx, cy, cz);
         const int begin = B.bucket_start[b], end = B.bucket_start[b + 1];
         for (int it = begin; it < end; ++it) {
+            if (B.bucket_key[it] != key) continue;
             const int q = B.bucket_items[it];
             if (q == p) continue;
-            const bm_v3 xq = ld3(pos, N, q);
-            if (cell_coord(xq.x, reach) != cx || cell_coord(xq.y, reach) != cy || cell_coord(xq.z, reach) != cz) continue;
+            const float4 xq4 = bpos[it];
+            const bm_v3 xq = v3(xq4.x, xq4.y, xq4.z);
             if (!(v3_len(v3_sub(xq, xp)) < reach)) continue;
-            if (compatible_codes(cp, B.codes[q]) && v3_len(v3_sub(rp, ld3(B.ref, N, q))) < 2.0f * P.spacing) continue;
+            if (v3_len(v3_sub(rp, ld3(B.ref, N, q))) < 2.0f * P.spacing && compatible_codes(cp, B.codes[q])) continue;
             if (count < 0) continue;
             if (count == BM_PAIR_LANES) {
                 count = -1;
@@ -588,14 +601,17 @@ __global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in) 
         const int p = B.changed[t];
         const bm_v3 xp = ld3(B.built_x, N, p);
         const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
+        const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
         if (atomicExch(&B.relist[p], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = p;
         for (int i = 0; i < 27; ++i) {
             const int cx = hx + i % 3 - 1, cy = hy + (i / 3) % 3 - 1, cz = hz + i / 9 - 1;
             const int b = list_bucket(cx, cy, cz, P.bucket_mask);
+            const int64_t key = cell_key(cx, cy, cz);
             for (int it = B.bucket_start[b]; it < B.bucket_start[b + 1]; ++it) {
+                if (B.bucket_key[it] != key) continue;
                 const int q = B.bucket_items[it];
-                const bm_v3 xq = ld3(B.built_x, N, q);
-                if (cell_coord(xq.x, reach) != cx || cell_coord(xq.y, reach) != cy || cell_coord(xq.z, reach) != cz) continue;
+                const float4 xq4 = bpos[it];
+                const bm_v3 xq = v3(xq4.x, xq4.y, xq4.z);
                 if (!(v3_len(v3_sub(xq, xp)) < reach)) continue;
                 if (atomicExch(&B.relist[q], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = q;
             }

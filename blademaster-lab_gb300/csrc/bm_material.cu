@@ -42,7 +42,11 @@ __device__ __forceinline__ void for_contributions(const bm_params& P, const bm_b
 __device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n);
 
 __global__ void k_register_begin(bm_buffers B, int force) {
-    if (force || B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0) B.flags[BM_FLAG_MULTI] = 0;
+    if (force || B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0) {
+        B.flags[BM_FLAG_MULTI] = 0;
+        B.flags[BM_FLAG_MIXED_CELLS] = 0;
+        B.flags[BM_FLAG_REGISTRATIONS] += 1;
+    }
 }
 
 __global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
@@ -117,9 +121,17 @@ __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 // absent particles and particles of another field contributing +0; a node
 // then adds the partials of its adjacent cells in ascending cell index
 // (corner index a = 7 .. 0), skipping cells without a particle of the field.
+//
+// The corner flags (cell_field[node][a]: the field of a uniform corner, 255
+// when the cell's particles map to different fields there, 254 when there is
+// no cell) depend only on the field indices, so registration writes them and
+// lists the cells with a mixed corner.  Per substep, the cell pass writes one
+// partial per corner; the mixed-cell pass writes, for each mixed corner, one
+// partial per field present (a "run"); single-field nodes read eight
+// partials, multi-field nodes are handled one warp each.
 
-constexpr int kMixed = 255;   // the cell's particles map to different fields at this corner
-constexpr int kAbsent = 254;  // no cell (outside the grid, or empty): set once at setup
+constexpr int kMixed = 255;
+constexpr int kAbsent = 254;
 constexpr unsigned kFull = 0xffffffffu;
 
 // Reduce-scatter over the 8 lanes of a cell group: vals[c][v] holds this
@@ -164,81 +176,47 @@ __device__ __forceinline__ int cell_at(const bm_params& P, int n, int a) {
     if (ci < 0 || cj < 0 || ck < 0 || ci >= P.cell_dims[0] || cj >= P.cell_dims[1] || ck >= P.cell_dims[2]) return -1;
     return (ci * P.cell_dims[1] + cj) * P.cell_dims[2] + ck;
 }
-
-// A cell group (8 lanes, mask gmask) with at least one mixed corner: for every
-// mixed corner, the tree sums of each field present (other lanes +0) are
-// appended to mixed_part as one run, ascending field; mixed_run[node][a]
-// records it (-1 when the buffer is full: the node pass then recomputes).
-template <int V>
-__device__ void emit_mixed_runs(const bm_params& P, const bm_buffers& B, const float (&vals)[8][V], uint64_t fidx,
-                                bool present, int base, unsigned gmask) {
-    const int s = threadIdx.x & 7;
-    const int lead = (threadIdx.x & 31) & ~7;
-    for (int a = 0; a < 8; ++a) {
-        const int f = present ? field_of(fidx, a) : 255;
-        int lo = f, hi = present ? f : -1;
-        for (int d = 1; d < 8; d <<= 1) {
-            lo = min(lo, __shfl_xor_sync(gmask, lo, d));
-            hi = max(hi, __shfl_xor_sync(gmask, hi, d));
-        }
-        if (lo == hi) continue;
-        int runs = 0;
-        for (int cur = lo; cur != 255;) {
-            ++runs;
-            int next = f > cur ? f : 255;
-            for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
-            cur = next;
-        }
-        int at = 0;
-        if (s == 0) at = atomicAdd(&B.flags[BM_FLAG_MIXED], runs);
-        at = __shfl_sync(gmask, at, lead);
-        const int node = base + node_offset(P, a);
-        const bool fits = at + runs <= P.mixed_capacity;
-        if (s == 0) B.mixed_run[node * 8 + a] = fits ? (at << 4) | runs : -1;
-        if (!fits) continue;
-        int k = 0;
-        for (int cur = lo; cur != 255; ++k) {
-            float out[V];
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                float x = f == cur ? vals[a][v] : 0.0f;
-                x = x + __shfl_xor_sync(gmask, x, 1);
-                x = x + __shfl_xor_sync(gmask, x, 2);
-                x = x + __shfl_xor_sync(gmask, x, 4);
-                out[v] = x;
-            }
-            if (s == 0) {
-                float* e = B.mixed_part + 8 * (at + k);
-#pragma unroll
-                for (int v = 0; v < V; ++v) e[v] = out[v];
-                e[7] = __int_as_float(cur);
-            }
-            int next = f > cur ? f : 255;
-            for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
-            cur = next;
-        }
-    }
+// Node of corner (0, 0, 0) of cell c.
+__device__ __forceinline__ int cell_base_node(const bm_params& P, int c) {
+    const int ck = c % P.cell_dims[2], cj = (c / P.cell_dims[2]) % P.cell_dims[1], ci = c / (P.cell_dims[1] * P.cell_dims[2]);
+    return (ci * P.node_dims[1] + cj) * P.node_dims[2] + ck;
 }
 
-// The run entry of field f at mixed corner (n, a); false if f has no
-// particle there; *missing when the run was not stored.
-__device__ __forceinline__ const float* mixed_entry(const bm_buffers& B, int n, int a, int f, bool* missing) {
-    const int run = B.mixed_run[n * 8 + a];
-    *missing = run < 0;
-    if (run < 0) return nullptr;
-    const int start = run >> 4, len = run & 15;
-    for (int k = 0; k < len; ++k) {
-        const float* e = B.mixed_part + 8 * (start + k);
-        if (__float_as_int(e[7]) == f) return e;
+// Registration, cell pass: corner flags of every occupied cell and the list of
+// cells with a mixed corner.  Thread (cell, slot); lane s decides corner s.
+__global__ void k_register_cells(bm_params P, bm_buffers B, int force) {
+    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+    const int cells = cell_count(P);
+    const int stride = gridDim.x * blockDim.x;
+    for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * cells; t0 += stride) {
+        const int t = t0 + threadIdx.x;
+        const int c = t >> 3, s = t & 7;
+        int count = 0, p = 0;
+        if (c < cells) {
+            const int b = B.cell_start[c];
+            count = B.cell_start[c + 1] - b;
+            p = b + s;
+        }
+        const uint64_t fidx = s < count ? B.fidx[p] : 0u;
+        const int group = threadIdx.x & 24;
+        int lo = kMixed, hi = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint64_t fk = __shfl_sync(kFull, fidx, group + k);
+            if (k < count) {
+                const int f = field_of(fk, s);
+                lo = min(lo, f);
+                hi = max(hi, f);
+            }
+        }
+        const bool mixed = count > 0 && lo != hi;
+        if (count > 0) B.cell_field[(cell_base_node(P, c) + node_offset(P, s)) * 8 + s] = (uint8_t)(mixed ? kMixed : lo);
+        const unsigned any = __ballot_sync(kFull, mixed);
+        if (s == 0 && ((any >> group) & 0xffu)) B.mixed_cells[atomicAdd(&B.flags[BM_FLAG_MIXED_CELLS], 1)] = c;
     }
-    return nullptr;
 }
 
 struct P2GContrib {
-    float m;
-    bm_v3 mom, J;
-};
-struct NodeSums {
     float m;
     bm_v3 mom, J;
 };
@@ -254,8 +232,8 @@ __device__ __forceinline__ P2GContrib p2g_contrib(const bm_params& P, const bm_b
     return c;
 }
 
-// Cell pass of p2g: thread (cell, slot); the 8-slot tree sums of every corner
-// written to cell_part[.][a][corner node] with the corner's field (or mixed).
+// Cell pass of p2g: thread (cell, slot); the 8-slot tree sum of every corner
+// written to cell_part[.][a][corner node] (meaningful where the corner is uniform).
 __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int cells = cell_count(P);
@@ -270,12 +248,10 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     const bool present = s < count;
     float vals[8][7];
     int base = 0;
-    uint64_t fidx = 0u;
     if (present) {
         const bm_v3 v = ld3(B.v, N, p), imp = ld3(B.impulses, N, p);
         const bm_m33 S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
         const int sid = B.stencil_id[p];
-        fidx = B.fidx[p];
         base = B.base_node[p];
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
@@ -296,110 +272,195 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     }
     float sum[7];
     reduce_scatter8<7>(vals, sum);
-    // the field of this lane's corner (a = s) over the group's particles
-    const int group = threadIdx.x & ~7;
-    int lo = kMixed, hi = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint64_t fk = __shfl_sync(kFull, fidx, group + k);
-        if (k < count) {
-            const int f = field_of(fk, s);
-            lo = min(lo, f);
-            hi = max(hi, f);
-        }
-    }
-    base = __shfl_sync(kFull, base, group);  // lane 0 of the group is present when count > 0
+    base = __shfl_sync(kFull, base, threadIdx.x & 24);  // lane 0 of the group is present when count > 0
     if (count > 0) {
-        const int node = base + node_offset(P, s), plane = 8 * NC;
-        float* part = B.cell_part + s * NC + node;
+        const int plane = 8 * NC;
+        float* part = B.cell_part + s * NC + base + node_offset(P, s);
 #pragma unroll
         for (int v = 0; v < 7; ++v) part[v * plane] = sum[v];
-        B.cell_field[node * 8 + s] = (uint8_t)(lo == hi ? lo : kMixed);
     }
-    const unsigned mixed = __ballot_sync(kFull, count > 0 && lo != hi);
-    if ((mixed >> (group & 31)) & 0xffu) emit_mixed_runs<7>(P, B, vals, fidx, present, base, 0xffu << (group & 31));
 }
 
-// The tree sum of field f over the particles of cell c at corner a (a cell
-// whose particles map to different fields there); false if none has f.
-__device__ __noinline__ bool p2g_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, P2GContrib* out) {
+// Per-field tree sums of the mixed corners of one cell (8 lanes, mask gmask),
+// appended to mixed_part as one run per corner (ascending field) and recorded
+// in mixed_run[node][a] (-1 when the buffer is full: the node pass then
+// recomputes that corner).
+template <int V>
+__device__ void emit_runs(const bm_params& P, const bm_buffers& B, const float (&vals)[V], int a, int f, int base,
+                          unsigned gmask) {
+    const int s = threadIdx.x & 7;
+    const int lead = threadIdx.x & 24;
+    int lo = f, hi = f == kMixed ? -1 : f;
+    for (int d = 1; d < 8; d <<= 1) {
+        lo = min(lo, __shfl_xor_sync(gmask, lo, d));
+        hi = max(hi, __shfl_xor_sync(gmask, hi, d));
+    }
+    if (lo == hi) return;
+    int runs = 0;
+    for (int cur = lo; cur != kMixed;) {
+        ++runs;
+        int next = f > cur ? f : kMixed;
+        for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
+        cur = next;
+    }
+    int at = 0;
+    if (s == 0) at = atomicAdd(&B.flags[BM_FLAG_MIXED], runs);
+    at = __shfl_sync(gmask, at, lead);
+    const int node = base + node_offset(P, a);
+    const bool fits = at + runs <= P.mixed_capacity;
+    if (s == 0) B.mixed_run[node * 8 + a] = fits ? (at << 4) | runs : -1;
+    if (!fits) return;
+    int k = 0;
+    for (int cur = lo; cur != kMixed; ++k) {
+        float out[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            float x = f == cur ? vals[v] : 0.0f;
+            x = x + __shfl_xor_sync(gmask, x, 1);
+            x = x + __shfl_xor_sync(gmask, x, 2);
+            x = x + __shfl_xor_sync(gmask, x, 4);
+            out[v] = x;
+        }
+        if (s == 0) {
+            float* e = B.mixed_part + 8 * (at + k);
+#pragma unroll
+            for (int v = 0; v < V; ++v) e[v] = out[v];
+            e[7] = __int_as_float(cur);
+        }
+        int next = f > cur ? f : kMixed;
+        for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
+        cur = next;
+    }
+}
+
+// Mixed-cell pass of p2g: 8 lanes per listed cell (warp-uniform loop).
+__global__ void __launch_bounds__(256) k_p2g_mixed_cells(bm_params P, bm_buffers B) {
+    const int listed = B.flags[BM_FLAG_MIXED_CELLS];
+    const int N = P.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * listed; t0 += stride) {
+        const int t = t0 + threadIdx.x;
+        const int j = t >> 3, s = t & 7;
+        const bool valid = j < listed;
+        const unsigned gmask = 0xffu << (threadIdx.x & 24);
+        if (!__any_sync(kFull, valid)) break;
+        if (!valid) continue;  // whole groups only: the group is valid or not
+        const int c = B.mixed_cells[j];
+        const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+        const bool present = s < count;
+        const int p = b + s, base = cell_base_node(P, c);
+        bm_v3 v = v3_zero(), imp = v3_zero();
+        bm_m33 S = m33_zero();
+        int sid = 0;
+        uint64_t fidx = 0u;
+        if (present) {
+            v = ld3(B.v, N, p);
+            imp = ld3(B.impulses, N, p);
+            S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
+            sid = B.stencil_id[p];
+            fidx = B.fidx[p];
+        }
+        for (int a = 0; a < 8; ++a) {
+            float vals[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (present) {
+                const P2GContrib k = p2g_contrib(P, B, v, imp, S, sid, a);
+                vals[0] = k.m;
+                vals[1] = k.mom.x;
+                vals[2] = k.mom.y;
+                vals[3] = k.mom.z;
+                vals[4] = k.J.x;
+                vals[5] = k.J.y;
+                vals[6] = k.J.z;
+            }
+            emit_runs<7>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask);
+        }
+    }
+}
+
+// The tree sum of field f over the particles of cell c at corner a when its
+// run was not stored; false if no particle of c has field f there.
+__device__ __noinline__ bool p2g_recompute(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
     const int N = P.n;
     const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-    P2GContrib slot[8];
+    float slot[8][7];
     bool any = false;
     for (int s = 0; s < 8; ++s) {
-        slot[s].m = 0.0f;
-        slot[s].mom = v3_zero();
-        slot[s].J = v3_zero();
+        for (int v = 0; v < 7; ++v) slot[s][v] = 0.0f;
         if (s < count && field_of(B.fidx[b + s], a) == f) {
             const int p = b + s;
-            slot[s] = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
-                                  m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
+            const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
+                                             m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
+            slot[s][0] = k.m;
+            slot[s][1] = k.mom.x;
+            slot[s][2] = k.mom.y;
+            slot[s][3] = k.mom.z;
+            slot[s][4] = k.J.x;
+            slot[s][5] = k.J.y;
+            slot[s][6] = k.J.z;
             any = true;
         }
     }
-    if (!any) return false;
-    P2GContrib r;
-    r.m = ((slot[0].m + slot[1].m) + (slot[2].m + slot[3].m)) + ((slot[4].m + slot[5].m) + (slot[6].m + slot[7].m));
-#define BM_TREE_V(field)                                                                                        \
-    v3(((slot[0].field.x + slot[1].field.x) + (slot[2].field.x + slot[3].field.x)) +                           \
-           ((slot[4].field.x + slot[5].field.x) + (slot[6].field.x + slot[7].field.x)),                        \
-       ((slot[0].field.y + slot[1].field.y) + (slot[2].field.y + slot[3].field.y)) +                           \
-           ((slot[4].field.y + slot[5].field.y) + (slot[6].field.y + slot[7].field.y)),                        \
-       ((slot[0].field.z + slot[1].field.z) + (slot[2].field.z + slot[3].field.z)) +                           \
-           ((slot[4].field.z + slot[5].field.z) + (slot[6].field.z + slot[7].field.z)))
-    r.mom = BM_TREE_V(mom);
-    r.J = BM_TREE_V(J);
-#undef BM_TREE_V
-    *out = r;
-    return true;
+    for (int v = 0; v < 7; ++v)
+        out[v] = ((slot[0][v] + slot[1][v]) + (slot[2][v] + slot[3][v])) + ((slot[4][v] + slot[5][v]) + (slot[6][v] + slot[7][v]));
+    return any;
 }
-
-// Node pass of p2g for field f: the adjacent cells' partials in ascending
-// cell index (a = 7 .. 0); mixed corners from their runs (or recomputed).
-__device__ NodeSums p2g_node_sums_multi(const bm_params& P, const bm_buffers& B, int n, int f) {
-    const int NC = P.node_count, plane = 8 * NC;
-    NodeSums r;
-    r.m = 0.0f;
-    r.mom = v3_zero();
-    r.J = v3_zero();
-    for (int a = 7; a >= 0; --a) {
-        const int flag = B.cell_field[n * 8 + a];
-        if (flag == f) {
-            const float* part = B.cell_part + a * NC + n;
-            r.m = r.m + part[0];
-            r.mom = v3_add(r.mom, v3(part[plane], part[2 * plane], part[3 * plane]));
-            r.J = v3_add(r.J, v3(part[4 * plane], part[5 * plane], part[6 * plane]));
-        } else if (flag == kMixed) {
-            bool missing;
-            const float* e = mixed_entry(B, n, a, f, &missing);
-            if (e) {
-                r.m = r.m + e[0];
-                r.mom = v3_add(r.mom, v3(e[1], e[2], e[3]));
-                r.J = v3_add(r.J, v3(e[4], e[5], e[6]));
-            } else if (missing) {
-                P2GContrib k;
-                if (p2g_mixed(P, B, cell_at(P, n, a), a, f, &k)) {
-                    r.m = r.m + k.m;
-                    r.mom = v3_add(r.mom, k.mom);
-                    r.J = v3_add(r.J, k.J);
-                }
-            }
+__device__ __noinline__ bool remap_recompute(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
+    const int N = P.n;
+    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+    float slot[8][3];
+    bool any = false;
+    for (int s = 0; s < 8; ++s) {
+        slot[s][0] = slot[s][1] = slot[s][2] = 0.0f;
+        if (s < count && field_of(B.fidx[b + s], a) == f) {
+            const bm_v3 r = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
+            slot[s][0] = r.x;
+            slot[s][1] = r.y;
+            slot[s][2] = r.z;
+            any = true;
         }
     }
-    return r;
+    for (int v = 0; v < 3; ++v)
+        out[v] = ((slot[0][v] + slot[1][v]) + (slot[2][v] + slot[3][v])) + ((slot[4][v] + slot[5][v]) + (slot[6][v] + slot[7][v]));
+    return any;
+}
+
+// Contribution of corner a of node n to field f (V sums): the uniform
+// partial, the mixed corner's run entry, or a recomputation; false if none.
+template <int V>
+__device__ __forceinline__ bool corner_value(const bm_params& P, const bm_buffers& B, int n, int a, int f, float* out) {
+    const int NC = P.node_count, plane = 8 * NC;
+    const int flag = B.cell_field[n * 8 + a];
+    if (flag == f) {
+        const float* part = B.cell_part + a * NC + n;
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = part[v * plane];
+        return true;
+    }
+    if (flag != kMixed) return false;
+    const int run = B.mixed_run[n * 8 + a];
+    if (run < 0) {
+        if (V == 7) return p2g_recompute(P, B, cell_at(P, n, a), a, f, out);
+        return remap_recompute(P, B, cell_at(P, n, a), a, f, out);
+    }
+    const int start = run >> 4, len = run & 15;
+    for (int k = 0; k < len; ++k) {
+        const float* e = B.mixed_part + 8 * (start + k);
+        if (__float_as_int(e[7]) == f) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) out[v] = e[v];
+            return true;
+        }
+    }
+    return false;
 }
 
 // p2g node sums + couple_and_velocity (material.py:127-152, 252-284) for the
 // single-field nodes, one thread per active node (a single-field node has no
-// mixed corner: every corner is field 0 or has no cell).  Also clears the
+// mixed corner: each corner is field 0 or has no cell).  Also clears the
 // topology flag consumed by registration and the mixed-run counter.
 __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) {
-        B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
-        B.flags[BM_FLAG_MIXED] = 0;  // the re-scatter's runs start over (p2g runs are read by k_p2g_multi only)
-    }
+    if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     if (B.nfield[n] != 1) return;
@@ -410,74 +471,98 @@ __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int
     for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int v = 0; v < 7; ++v) part[a][v] = B.cell_part[v * plane + a * NC + n];
-    NodeSums s;
-    s.m = 0.0f;
-    s.mom = v3_zero();
-    s.J = v3_zero();
+    float m = 0.0f;
+    bm_v3 mom = v3_zero(), J = v3_zero();
 #pragma unroll
     for (int a = 7; a >= 0; --a) {
         if (((flags >> (8 * a)) & 0xffu) != 0u) continue;  // no cell at this corner
-        s.m = s.m + part[a][0];
-        s.mom = v3_add(s.mom, v3(part[a][1], part[a][2], part[a][3]));
-        s.J = v3_add(s.J, v3(part[a][4], part[a][5], part[a][6]));
+        m = m + part[a][0];
+        mom = v3_add(mom, v3(part[a][1], part[a][2], part[a][3]));
+        J = v3_add(J, v3(part[a][4], part[a][5], part[a][6]));
     }
-    B.grid_mass[n] = s.m;
+    B.grid_mass[n] = m;
     if (write_sums) {
-        st3(B.momentum, S, n, s.mom);
-        st3(B.grid_impulse, S, n, s.J);
+        st3(B.momentum, S, n, mom);
+        st3(B.grid_impulse, S, n, J);
     }
-    if (s.m <= 0.0f) {
+    if (m <= 0.0f) {
         st3(B.old_v, S, n, v3_zero());
         st3(B.new_v, S, n, v3_zero());
         return;
     }
-    const bm_v3 pm = v3_add(s.mom, v3_div(v3_zero(), s.m));
-    const bm_v3 jm = v3_add(s.J, v3_div(v3_zero(), s.m));
-    st3(B.old_v, S, n, v3_div(pm, s.m));
-    st3(B.new_v, S, n, v3_div(v3_add(pm, jm), s.m));
+    const bm_v3 pm = v3_add(mom, v3_div(v3_zero(), m));
+    const bm_v3 jm = v3_add(J, v3_div(v3_zero(), m));
+    st3(B.old_v, S, n, v3_div(pm, m));
+    st3(B.new_v, S, n, v3_div(v3_add(pm, jm), m));
 }
 
-// The nodes with several fields (listed at registration): field sums and the
-// exchange of couple_and_velocity (material.py:252-284).
+// Multi-field nodes, one warp per listed node: lane (field f, corner a)
+// fetches one corner value, then the lane of corner 0 of each field adds the
+// eight in ascending cell index (a = 7 .. 0); fields are taken four at a time.
+// Then lane f evaluates the exchange of field f (couple_and_velocity_at).
 __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
     const int count = B.flags[BM_FLAG_MULTI];
     const int S = P.fmax * P.node_count;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        const int n = B.multi_nodes[t];
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < count; w += warps) {
+        const int n = B.multi_nodes[w];
         const int nf = B.nfield[n];
-        for (int f = 0; f < nf; ++f) {
-            const NodeSums s = p2g_node_sums_multi(P, B, n, f);
-            const int slot = f * P.node_count + n;
-            B.grid_mass[slot] = s.m;
-            st3(B.momentum, S, slot, s.mom);
-            st3(B.grid_impulse, S, slot, s.J);
+        // sums: grid_mass, momentum (3), grid_impulse (3) through one store layout
+        const int lanef = lane >> 3, a = lane & 7;
+        for (int f0 = 0; f0 < nf; f0 += 4) {
+            const int f = f0 + lanef;
+            float val[7];
+            bool have = false;
+            if (f < nf) have = corner_value<7>(P, B, n, a, f, val);
+            if (!have)
+                for (int v = 0; v < 7; ++v) val[v] = 0.0f;
+            const unsigned haves = __ballot_sync(kFull, have);
+            float sum[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            for (int c = 7; c >= 0; --c) {
+                const int src = (lane & 24) + c;
+                const bool use = (haves >> src) & 1u;
+                for (int v = 0; v < 7; ++v) {
+                    const float x = __shfl_sync(kFull, val[v], src);
+                    if (use) sum[v] = sum[v] + x;
+                }
+            }
+            if (a == 0 && f < nf) {
+                const int slot = f * P.node_count + n;
+                B.grid_mass[slot] = sum[0];
+                st3(B.momentum, S, slot, v3(sum[1], sum[2], sum[3]));
+                st3(B.grid_impulse, S, slot, v3(sum[4], sum[5], sum[6]));
+            }
         }
-        for (int f = 0; f < nf; ++f) {
-            const int a = f * P.node_count + n;
-            const float ma = B.grid_mass[a];
+        __syncwarp();
+        // exchange (couple_and_velocity_at): lane f handles field f
+        for (int f = lane; f < nf; f += 32) {
+            const int sa = f * P.node_count + n;
+            const float ma = B.grid_mass[sa];
             if (ma <= 0.0f) {
-                st3(B.old_v, S, a, v3_zero());
-                st3(B.new_v, S, a, v3_zero());
+                st3(B.old_v, S, sa, v3_zero());
+                st3(B.new_v, S, sa, v3_zero());
                 continue;
             }
-            const bm_v3 pa = ld3(B.momentum, S, a), ja = ld3(B.grid_impulse, S, a);
-            const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+            const bm_v3 pa = ld3(B.momentum, S, sa), ja = ld3(B.grid_impulse, S, sa);
+            const uint64_t oa = B.fones[sa], ta = B.ftwos[sa];
             float total = 0.0f;
             bm_v3 dm = v3_zero(), di = v3_zero();
             for (int g = 0; g < nf; ++g) {
-                const int b = g * P.node_count + n;
-                const float mb = B.grid_mass[b];
+                const int sb = g * P.node_count + n;
+                const float mb = B.grid_mass[sb];
                 total = total + mb;
-                if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b])) {
-                    dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, b), ma), v3_mul(pa, mb)));
-                    di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, b), ma), v3_mul(ja, mb)));
+                if (g != f && compatible_masks(oa, ta, B.fones[sb], B.ftwos[sb])) {
+                    dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, sb), ma), v3_mul(pa, mb)));
+                    di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, sb), ma), v3_mul(ja, mb)));
                 }
             }
             const bm_v3 pm = v3_add(pa, v3_div(dm, total));
             const bm_v3 jm = v3_add(ja, v3_div(di, total));
-            st3(B.old_v, S, a, v3_div(pm, ma));
-            st3(B.new_v, S, a, v3_div(v3_add(pm, jm), ma));
+            st3(B.old_v, S, sa, v3_div(pm, ma));
+            st3(B.new_v, S, sa, v3_div(v3_add(pm, jm), ma));
         }
+        __syncwarp();
     }
 }
 
@@ -488,6 +573,7 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
 // partials of the MUSL re-scatter (material.py:400-401), thread (cell, slot).
 __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // runs of the re-scatter start over (p2g runs are consumed)
     const int cells = cell_count(P);
     const int c = t >> 3, s = t & 7;
     const int N = P.n, S = P.fmax * P.node_count, NC = P.node_count;
@@ -533,75 +619,60 @@ __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float ha
     }
     float sum[3];
     reduce_scatter8<3>(vals, sum);
-    const int group = threadIdx.x & ~7;
-    base = __shfl_sync(kFull, base, group);
-    bool mixed_corner = false;
+    base = __shfl_sync(kFull, base, threadIdx.x & 24);
     if (count > 0) {
-        const int node = base + node_offset(P, s);
-        float* part = B.cell_part + s * NC + node;
+        float* part = B.cell_part + s * NC + base + node_offset(P, s);
         const int plane = 8 * NC;
         part[0] = sum[0];
         part[plane] = sum[1];
         part[2 * plane] = sum[2];
-        mixed_corner = B.cell_field[node * 8 + s] == kMixed;
     }
-    const unsigned mixed = __ballot_sync(kFull, mixed_corner);
-    if ((mixed >> (group & 31)) & 0xffu) {
-        uint64_t fidx = present ? B.fidx[p] : 0u;
-        emit_mixed_runs<3>(P, B, vals, fidx, present, base, 0xffu << (group & 31));
+}
+
+// Mixed-cell pass of the re-scatter (new particle velocities).
+__global__ void __launch_bounds__(256) k_remap_mixed_cells(bm_params P, bm_buffers B) {
+    const int listed = B.flags[BM_FLAG_MIXED_CELLS];
+    const int N = P.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * listed; t0 += stride) {
+        const int t = t0 + threadIdx.x;
+        const int j = t >> 3, s = t & 7;
+        const bool valid = j < listed;
+        const unsigned gmask = 0xffu << (threadIdx.x & 24);
+        if (!__any_sync(kFull, valid)) break;
+        if (!valid) continue;
+        const int c = B.mixed_cells[j];
+        const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+        const bool present = s < count;
+        const int p = b + s, base = cell_base_node(P, c);
+        bm_v3 v = v3_zero();
+        int sid = 0;
+        uint64_t fidx = 0u;
+        if (present) {
+            v = ld3(B.v, N, p);
+            sid = B.stencil_id[p];
+            fidx = B.fidx[p];
+        }
+        for (int a = 0; a < 8; ++a) {
+            float vals[3] = {0.0f, 0.0f, 0.0f};
+            if (present) {
+                const bm_v3 r = v3_mul(v, P.mass * stencil_w(B, sid, a));
+                vals[0] = r.x;
+                vals[1] = r.y;
+                vals[2] = r.z;
+            }
+            emit_runs<3>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask);
+        }
     }
 }
 
 // ---------------------------------------------------------- remap + couple
 
-// Tree sum of the remap contributions of field f over cell c at corner a.
-__device__ __noinline__ bool remap_mixed(const bm_params& P, const bm_buffers& B, int c, int a, int f, bm_v3* out) {
-    const int N = P.n;
-    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-    bm_v3 slot[8];
-    bool any = false;
-    for (int s = 0; s < 8; ++s) {
-        slot[s] = v3_zero();
-        if (s < count && field_of(B.fidx[b + s], a) == f) {
-            slot[s] = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
-            any = true;
-        }
-    }
-    if (!any) return false;
-    *out = v3(((slot[0].x + slot[1].x) + (slot[2].x + slot[3].x)) + ((slot[4].x + slot[5].x) + (slot[6].x + slot[7].x)),
-              ((slot[0].y + slot[1].y) + (slot[2].y + slot[3].y)) + ((slot[4].y + slot[5].y) + (slot[6].y + slot[7].y)),
-              ((slot[0].z + slot[1].z) + (slot[2].z + slot[3].z)) + ((slot[4].z + slot[5].z) + (slot[6].z + slot[7].z)));
-    return true;
-}
-
-// Remap sums of field f at node n (multi-field nodes): partials, runs, or recomputed.
-__device__ bm_v3 remap_node_sum_multi(const bm_params& P, const bm_buffers& B, int n, int f) {
-    const int NC = P.node_count, plane = 8 * NC;
-    bm_v3 r = v3_zero();
-    for (int a = 7; a >= 0; --a) {
-        const int flag = B.cell_field[n * 8 + a];
-        if (flag == f) {
-            const float* part = B.cell_part + a * NC + n;
-            r = v3_add(r, v3(part[0], part[plane], part[2 * plane]));
-        } else if (flag == kMixed) {
-            bool missing;
-            const float* e = mixed_entry(B, n, a, f, &missing);
-            if (e) {
-                r = v3_add(r, v3(e[0], e[1], e[2]));
-            } else if (missing) {
-                bm_v3 k;
-                if (remap_mixed(P, B, cell_at(P, n, a), a, f, &k)) r = v3_add(r, k);
-            }
-        }
-    }
-    return r;
-}
-
 // Node pass of the MUSL re-scatter, then couple (material.py:155-193) for the
 // single-field nodes; stores coupled / mass for the F update.
 __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // the next p2g's runs start over
+    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // the next p2g's runs start over (re-scatter runs are read by k_remap_multi)
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     if (B.nfield[n] != 1) return;
@@ -630,30 +701,52 @@ __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B)
 __global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) {
     const int count = B.flags[BM_FLAG_MULTI];
     const int S = P.fmax * P.node_count;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        const int n = B.multi_nodes[t];
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < count; w += warps) {
+        const int n = B.multi_nodes[w];
         const int nf = B.nfield[n];
-        for (int f = 0; f < nf; ++f) st3(B.remapped, S, f * P.node_count + n, remap_node_sum_multi(P, B, n, f));
-        for (int f = 0; f < nf; ++f) {
-            const int a = f * P.node_count + n;
-            const float ma = B.grid_mass[a];
+        const int lanef = lane >> 3, a = lane & 7;
+        for (int f0 = 0; f0 < nf; f0 += 4) {
+            const int f = f0 + lanef;
+            float val[3];
+            bool have = false;
+            if (f < nf) have = corner_value<3>(P, B, n, a, f, val);
+            if (!have) val[0] = val[1] = val[2] = 0.0f;
+            const unsigned haves = __ballot_sync(kFull, have);
+            float sum[3] = {0.0f, 0.0f, 0.0f};
+            for (int c = 7; c >= 0; --c) {
+                const int src = (lane & 24) + c;
+                const bool use = (haves >> src) & 1u;
+                for (int v = 0; v < 3; ++v) {
+                    const float x = __shfl_sync(kFull, val[v], src);
+                    if (use) sum[v] = sum[v] + x;
+                }
+            }
+            if (a == 0 && f < nf) st3(B.remapped, S, f * P.node_count + n, v3(sum[0], sum[1], sum[2]));
+        }
+        __syncwarp();
+        for (int f = lane; f < nf; f += 32) {
+            const int sa = f * P.node_count + n;
+            const float ma = B.grid_mass[sa];
             if (ma <= 0.0f) {
-                st3(B.remap_v, S, a, v3_zero());
+                st3(B.remap_v, S, sa, v3_zero());
                 continue;
             }
-            const bm_v3 sa = ld3(B.remapped, S, a);
-            const uint64_t oa = B.fones[a], ta = B.ftwos[a];
+            const bm_v3 va = ld3(B.remapped, S, sa);
+            const uint64_t oa = B.fones[sa], ta = B.ftwos[sa];
             float total = 0.0f;
             bm_v3 ex = v3_zero();
             for (int g = 0; g < nf; ++g) {
-                const int b = g * P.node_count + n;
-                const float mb = B.grid_mass[b];
+                const int sb = g * P.node_count + n;
+                const float mb = B.grid_mass[sb];
                 total = total + mb;
-                if (g != f && compatible_masks(oa, ta, B.fones[b], B.ftwos[b]))
-                    ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, b), ma), v3_mul(sa, mb)));
+                if (g != f && compatible_masks(oa, ta, B.fones[sb], B.ftwos[sb]))
+                    ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, sb), ma), v3_mul(va, mb)));
             }
-            st3(B.remap_v, S, a, v3_div(v3_add(sa, v3_div(ex, total)), ma));
+            st3(B.remap_v, S, sa, v3_div(v3_add(va, v3_div(ex, total)), ma));
         }
+        __syncwarp();
     }
 }
 
@@ -1011,20 +1104,24 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
     const unsigned wide = 8 * 152;  // grid-stride: cheap to launch when the gate is off
     const unsigned gn = grid_for(P.active_nodes) < wide ? grid_for(P.active_nodes) : wide;
     const unsigned gp = grid_for(P.n) < wide ? grid_for(P.n) : wide;
+    const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
+    const unsigned gc = grid_for(cells8) < wide ? grid_for(cells8) : wide;
     k_register_begin<<<1, 1, 0, st>>>(s->B, force);
     k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes, force);
     k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes, force);
+    k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B, force);
 }
 
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
-    const int S = P.fmax * P.node_count;
+    const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
+    k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
+    k_p2g_mixed_cells<<<2 * 152, kBlock, 0, st>>>(P, B);
+    k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
+    k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B);
     if (P.viscous) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
-        k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
-        k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, 1);
-        k_p2g_multi<<<2 * 152, kBlock, 0, st>>>(P, B);
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.grid_impulse);
         k_viscous_stress<<<grid_for(P.n), kBlock, 0, st>>>(P, B, s->viscous_scratch);
@@ -1032,24 +1129,20 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
         // coupled impulse into remap_v as scratch (overwritten by the remap below)
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.grid_impulse, B.remap_v);
         k_grid_vel<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.remapped, B.remap_v);
-        (void)S;
-    } else {
-        k_p2g_cells<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(P, B);
-        k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, write_sums);
-        k_p2g_multi<<<2 * 152, kBlock, 0, st>>>(P, B);
     }
 }
 
 void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
-    k_g2p<<<grid_for(8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2]), kBlock, 0, st>>>(
-        P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
+    const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
+    k_g2p<<<grid_for(cells8), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
+    k_remap_mixed_cells<<<2 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
 void launch_remap(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
     k_remap_couple<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B);
-    k_remap_multi<<<2 * 152, kBlock, 0, st>>>(P, s->B);
+    k_remap_multi<<<4 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
 void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,

@@ -134,6 +134,7 @@ typedef struct bm_buffers {
     int32_t* mixed_run;  /* [node_count][8] start << 4 | length of a mixed corner's per-field partials, -1 none */
     float* mixed_part;   /* [mixed_capacity][8] per-field partials of mixed corners (7 sums, field as float) */
     int32_t* multi_nodes;/* [active_nodes] nodes with more than one field */
+    int32_t* mixed_cells;/* [cells] cells whose particles map to different fields at some corner */
     /* pair contact */
     float* built_x;      /* [3][n] */
     int64_t* built_codes;/* [n] */
@@ -144,6 +145,9 @@ typedef struct bm_buffers {
     int32_t* bucket_items;  /* [n] */
     int32_t* bucket_fill;   /* [buckets] */
     int32_t* particle_bucket; /* [n] */
+    int64_t* particle_key;  /* [n] packed cell of the particle at the last build */
+    int64_t* bucket_key;    /* [n] packed cell of each bucket item */
+    float* bucket_pos;      /* [n][4] position of each bucket item at the last build */
     int64_t* pair_keys;  /* [2][pair_capacity] */
     float* pair_history; /* [2][pair_capacity][3] */
     int32_t* pair_used;  /* [2][pair_capacity] */
@@ -189,7 +193,9 @@ typedef struct bm_buffers {
 #define BM_FLAG_RELIST 8         /* entries of buffers.relist_list */
 #define BM_FLAG_MULTI 9          /* entries of buffers.multi_nodes */
 #define BM_FLAG_MIXED 10         /* entries of buffers.mixed_part in use */
-#define BM_FLAG_WORDS 12
+#define BM_FLAG_MIXED_CELLS 11   /* entries of buffers.mixed_cells */
+#define BM_FLAG_REGISTRATIONS 12 /* topology registrations run */
+#define BM_FLAG_WORDS 16
 
 typedef struct bm_solver bm_solver;
 typedef struct bm_graph bm_graph;
