@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_capi.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_capi.cu", "bm_noalloc.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -157,6 +157,7 @@ def _declare(lib):
         "bm_material_step": ([vp, i, vp], i),
         "bm_rigid_contacts": ([vp, i, vp], i),
         "bm_particle_contacts": ([vp, vp], i),
+        "bm_particle_contacts_static": ([vp, vp], i),
         "bm_assign_sides": ([vp, i, i, vp], i),
         "bm_drive_tool": ([vp, i, vp], i),
         "bm_finish_external": ([vp, vp], i),

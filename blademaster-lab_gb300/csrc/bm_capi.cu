@@ -12,8 +12,10 @@
 #include "bm_internal.h"
 
 namespace {
-
 thread_local std::string g_error;
+}  // namespace
+
+namespace bm {
 
 int fail(int code, const char* what) {
     g_error = what;
@@ -28,6 +30,13 @@ int check_cuda(const char* where) {
     }
     return BM_OK;
 }
+
+}  // namespace bm
+
+namespace {
+
+using bm::check_cuda;
+using bm::fail;
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

@@ -774,13 +774,14 @@ void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st) {
     k_rigid<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, cut_bits);
 }
 
-void launch_pairs(const bm_solver* s, cudaStream_t st) {
+void launch_pairs(const bm_solver* s, cudaStream_t st) { launch_pairs_using(s, s->scan_partials, st); }
+
+void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
     const int force = P.pair_search != 0;
     const int32_t* gate = force ? nullptr : &B.flags[BM_FLAG_PAIR_DIRTY];
     float* reach = reinterpret_cast<float*>(B.scratch);
-    int32_t* partials = s->scan_partials;
     const int64_t buckets = s->buckets;
     const int64_t tiles = (buckets + 1023) / 1024;
     const unsigned wide = 4 * 152;  // grid-stride: cheap to launch when the gate is off

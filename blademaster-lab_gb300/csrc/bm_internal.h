@@ -34,6 +34,9 @@ void launch_plastic_project(float* F, float* Fp, int n, float mu, float yield_st
 void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st);
 void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st);
 void launch_pairs(const bm_solver* s, cudaStream_t st);
+// The same launches with the bucket-scan partials (one int per 1024 buckets,
+// written before they are read) at `partials`.
+void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st);
 void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st);
 void launch_blade_query(const float* local, int n, const float* half, float bevel, float* closest, float* normal,
                         float* distance, cudaStream_t st);
@@ -60,6 +63,12 @@ void launch_couple_probe(const int64_t* codes, const float* mass, const float* s
                          int nodes, float* result, cudaStream_t st);
 void launch_g2p_probe(float* x, float* v, const int32_t* slots, const float* weights, const float* old_v,
                       const float* new_v, int n, float dt, float flip, cudaStream_t st);
+
+// C-ABI error reporting shared by the entry-point translation units: records
+// `what` for bm_last_error and returns `code`; check_cuda turns a pending CUDA
+// error into BM_ERR_CUDA with `where` in the message.
+int fail(int code, const char* what);
+int check_cuda(const char* where);
 
 // Tool kernel modes.
 enum ToolMode { kToolDrive = 0, kToolFinishExternal = 1, kToolAccumulate = 2, kToolClear = 3 };

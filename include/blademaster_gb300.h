@@ -238,6 +238,19 @@ int bm_material_step(bm_solver* s, int single_field, void* stream);
 int bm_rigid_contacts(bm_solver* s, int cut_bits, void* stream);
 /* Solver.particle_contacts (solver.py:670-751): pair contact with friction history. */
 int bm_particle_contacts(bm_solver* s, void* stream);
+/* bm_particle_contacts with the bucket-scan workspace of the pair-list rebuild
+ * in a static device array of BM_STATIC_SCAN_PARTIALS ints (64 KiB) instead of
+ * buffers.scratch; it allocates nothing.  No counterpart in the reference: it
+ * serves hosts that step the contact pass inside their own frame loop under a
+ * device-memory budget fixed at start-up, where an allocation would stall or
+ * fail.  Limit: pair-list tables of at most 1024 * BM_STATIC_SCAN_PARTIALS
+ * buckets (bucket_mask + 1), else BM_ERR_ARGUMENT.  The first call on each
+ * device (the current one) looks up the array's address and should come
+ * before any stream capture.  Calls that overlap on one device (two streams,
+ * solvers or host threads) share the array and race: serialise them.
+ * Results equal bm_particle_contacts'. */
+#define BM_STATIC_SCAN_PARTIALS 16384
+int bm_particle_contacts_static(bm_solver* s, void* stream);
 /* Solver.assign_sides (solver.py:866-890). */
 int bm_assign_sides(bm_solver* s, int cut_index, int cutting, void* stream);
 /* Solver._drive_tool (solver.py:824-864): targets/rotations row `index`. */
