@@ -114,6 +114,9 @@ def lib():
 
 
 def ptr(a):
+    """Address of a C-contiguous array's data (the caller keeps the array alive across the call)."""
+    if not a.flags.c_contiguous:
+        raise ValueError("oracle arrays must be C-contiguous")
     return ctypes.c_void_p(a.ctypes.data)
 
 
