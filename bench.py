@@ -21,6 +21,7 @@ the GPU machine and refuses CPU devices, blademaster_warp/solver.py:161-162).
 """
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -246,8 +247,17 @@ def main():
             done += k
 
     run(args.warmup)
-    if args.steps % batch and not args.eager:
-        s.prepare(zeros[: args.steps % batch], True, 0)  # capture outside the timed region
+
+    def graph_kernels(k):
+        """Kernel launches of one replay of the k-substep graph (its kernel nodes)."""
+        count = ctypes.c_int64()
+        _native.check(s._lib.bm_graph_kernel_count(s.prepare(zeros[:k], True, 0), ctypes.byref(count)))
+        return count.value
+
+    # graphs are captured outside the timed region; eager runs launch the same kernels
+    timed_launches = (args.steps // batch) * graph_kernels(batch)
+    if args.steps % batch:
+        timed_launches += graph_kernels(args.steps % batch)
     torch.cuda.synchronize()
     clock_file = tempfile.NamedTemporaryFile(suffix=".csv", delete=False).name
     sampler = sample_clocks(clock_file)
@@ -283,10 +293,10 @@ def main():
     value = world * s.n * args.steps / (ms / 1e3)
 
     # per-stage device time (CUDA events around each stage, eager launches)
-    stage_ms = (ctypes_array := __import__("ctypes").c_float * len(_native.STAGES))()
+    stage_ms = (ctypes.c_float * len(_native.STAGES))()
     a = s._step_args(args.profile_steps, True, 0, use_targets=0)
     s._flag("STEP", s.step_count)
-    _native.check(s._lib.bm_substeps_profiled(s._handle, __import__("ctypes").byref(a), stage_ms, s._stream))
+    _native.check(s._lib.bm_substeps_profiled(s._handle, ctypes.byref(a), stage_ms, s._stream))
     s.step_count += args.profile_steps
     stages = {name: stage_ms[i] / args.profile_steps for i, name in enumerate(_native.STAGES)}
     dominant = max(STAGE_BYTES, key=lambda k: stages[k])
@@ -357,8 +367,7 @@ def main():
         "device_errors": errors,
         "timed_region_events": events,
     }
-    launches_per_substep = 19
-    line["gpu_launches"] = launches_per_substep * args.steps
+    line["gpu_launches"] = timed_launches
     clocks = summarize_clocks(clock_file, torch.cuda.current_device()) if sampler else None
     line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -134,7 +134,7 @@ TOOL_F_WORDS = int(header_constant("BM_TOOL_F_WORDS"))
 FLAG = {
     k: int(header_constant("BM_FLAG_" + k))
     for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "CHANGED",
-              "RELIST", "MULTI", "MIXED", "MIXED_CELLS", "REGISTRATIONS", "WORDS")
+              "RELIST", "MULTI", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "WORDS")
 }
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
 STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate"]
@@ -168,6 +168,7 @@ def _declare(lib):
         "bm_substeps_profiled": ([vp, ctypes.POINTER(StepArgs), vp, vp], i),
         "bm_graph_launch": ([vp, vp], i),
         "bm_graph_destroy": ([vp], i),
+        "bm_graph_kernel_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "bm_count_embedded": ([vp, i, vp], i),
         "bm_validate_interval": ([vp, vp], i),
         "bm_read_accumulators": ([vp, vp, vp, vp, vp, vp], i),

@@ -7,6 +7,7 @@
 
 #include <new>
 #include <string>
+#include <vector>
 
 #include "bm_device.cuh"
 #include "bm_internal.h"
@@ -333,6 +334,22 @@ int bm_graph_destroy(bm_graph* g) {
     cudaGraphExecDestroy(g->exec);
     cudaGraphDestroy(g->graph);
     delete g;
+    return BM_OK;
+}
+
+int bm_graph_kernel_count(const bm_graph* g, int64_t* count) {
+    if (!g || !count) return fail(BM_ERR_ARGUMENT, "null argument");
+    size_t n = 0;
+    if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return check_cuda("graph nodes");
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return check_cuda("graph nodes");
+    int64_t kernels = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType type;
+        if (cudaGraphNodeGetType(nodes[i], &type) != cudaSuccess) return check_cuda("graph node type");
+        if (type == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    *count = kernels;
     return BM_OK;
 }
 

@@ -259,6 +259,41 @@ __device__ __forceinline__ void warp_accumulate3(uint64_t* acc, bm_v3 v, bool an
     warp_accumulate(acc + 4, bm_fx_from_float(v.z));
 }
 
+// Knives that may be in contact with some particle of this block (the same
+// mask in every thread).  A knife is left out when, on one of its axes, the
+// block's bounding box lies farther from it than blade_at's per-particle axis
+// pre-test allows at the block's largest particle speed, plus 1 um for
+// rounding: every particle of the block then takes blade_at's "far" outcome.
+// Thread 0 also raises the substep's maximum particle speed (one atomic per
+// block; rigid_and_speed's atomic_max, contact.py:497).
+__device__ unsigned rigid_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, float speed, bool active,
+                                 float radius_of_blade) {
+    __shared__ unsigned knives;
+    bm_v3 c, e;
+    float vmax;
+    bool any;
+    block_box(x, speed, active, &c, &e, &vmax, &any);
+    if (threadIdx.x == 0) {
+        knives = 0u;
+        if (any) atomic_max_nonneg(B.speed, vmax);
+    }
+    __syncthreads();
+    const int k = threadIdx.x;
+    if (any && k < P.tool_count) {
+        const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
+        const float max_closing = (vmax + T.speed) + T.spin_reach;
+        const float margin = (P.blade_offset + P.dt * max_closing) * 1.01f + 1.0e-6f;
+        const float axis_margin = margin + 1.0e-5f * radius_of_blade + 1.0e-6f;
+        const bm_v3 d = v3_sub(c, T.pos);
+        const bool far = fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) - P.half[0] > axis_margin ||
+                         fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) - P.half[1] > axis_margin ||
+                         fabsf(v3_dot(d, T.az)) - box_reach(T.az, e) - P.half[2] > axis_margin;
+        if (!far) atomicOr(&knives, 1u << k);
+    }
+    __syncthreads();
+    return knives;
+}
+
 // contact.rigid_and_speed + extra_blade (contact.py:422-566) for every knife.
 __global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,7 +327,17 @@ __global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
         }
     }
     warp_accumulate3(B.acc + BM_ACC_BOARD, jb, board_hit);
+    const unsigned knives = rigid_knives(P, B, xp, speed, active, radius_of_blade);
     for (int k = 0; k < P.tool_count; ++k) {
+        if (((knives >> k) & 1u) == 0u) {
+            // no particle of the block is near knife k: blade_at's far outcome
+            const unsigned bit = 1u << (1 + k);
+            if (active && (mask & bit)) {
+                st3(B.histories + (int64_t)(1 + k) * 3 * N, N, p, v3_zero());
+                mask &= ~bit;
+            }
+            continue;
+        }
         bm_v3 reaction = v3_zero(), torque = v3_zero();
         if (active) {
             const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
@@ -308,9 +353,6 @@ __global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
         st3(B.impulses, N, p, total);
         if (mask != mask_in) B.hist_mask[p] = (uint16_t)mask;
     }
-    // maximum speed: warp max, then one atomic per warp
-    for (int d = 16; d > 0; d >>= 1) speed = fmaxf(speed, __shfl_xor_sync(0xffffffffu, speed, d));
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(B.speed, speed);
 }
 
 // ------------------------------------------------------------ pair contact
@@ -446,6 +488,19 @@ __global__ void k_pair_setup(bm_params P, bm_buffers B, float* reach_out, int fo
     B.flags[BM_FLAG_CANDIDATES] = 0;
     B.flags[BM_FLAG_PAIR_BUILDS] += 1;
     B.flags[BM_FLAG_CHANGED] = 0;  // a full build uses the current codes
+    B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f, raised by k_max_disp
+}
+
+// Largest displacement |x - ref| over all particles, for the build's
+// reference-distance bound (see build_list).
+__global__ void k_max_disp(bm_params P, bm_buffers B, const int32_t* gate_flag) {
+    if (gate_flag && *gate_flag == 0) return;
+    const int N = P.n;
+    float d = 0.0f;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
+        d = fmaxf(d, v3_len(v3_sub(ld3(B.x, N, p), ld3(B.ref, N, p))));
+    for (int s = 16; s > 0; s >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, s));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_MAX_DISP]), d);
 }
 
 __global__ void k_zero_i32(int32_t* a, int64_t n, const int32_t* gate_flag) {
@@ -548,6 +603,20 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
     const int64_t cp = B.codes[p];
     if (pos == B.x) st3(B.built_x, N, p, xp);
     B.built_codes[p] = cp;
+    // A particle without cut digits is compatible with every code, so its only
+    // possible partners are particles farther than 2 h from it in the
+    // reference configuration.  Any particle q within the reach has
+    // |ref_p - ref_q| <= |x_p - ref_p| + reach + |x_q - ref_q|, and the last
+    // term is at most the build's largest displacement: when that sum stays
+    // below 2 h (less 0.1 % for rounding) the list is empty without a search.
+    if (cp == 0) {
+        const float largest = __int_as_float(B.flags[BM_FLAG_MAX_DISP]);
+        if ((v3_len(v3_sub(xp, rp)) + largest) + reach < 0.999f * (2.0f * P.spacing)) {
+            B.partner_count[p] = 0;
+            if (pos == B.x) B.listed[p] = 0;
+            return;
+        }
+    }
     const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
     int32_t* list = B.partners + (int64_t)p * BM_PAIR_LANES;
     const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
@@ -789,6 +858,7 @@ void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) 
     const unsigned gn = grid_for(P.n) < wide ? grid_for(P.n) : wide;
     const unsigned gt = tiles < 152 ? (unsigned)tiles : 152;
     k_pair_setup<<<1, 1, 0, st>>>(P, B, reach, force);
+    k_max_disp<<<gn, kBlock, 0, st>>>(P, B, gate);
     k_zero_i32<<<gb, kBlock, 0, st>>>(B.bucket_fill, buckets, gate);
     k_bin_count<<<gn, kBlock, 0, st>>>(P, B, reach, gate);
     k_scan_tiles<<<gt, 1024, 0, st>>>(B.bucket_fill, B.bucket_start, buckets, partials, gate);

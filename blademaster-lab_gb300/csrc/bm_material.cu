@@ -282,34 +282,27 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
 }
 
 // Per-field tree sums of the mixed corners of one cell (8 lanes, mask gmask),
-// appended to mixed_part as one run per corner (ascending field) and recorded
-// in mixed_run[node][a] (-1 when the buffer is full: the node pass then
-// recomputes that corner).
+// written to mixed_part as one run per corner (ascending field, at most 8
+// fields) in the fixed region of 8 entries that starts at `region`, and
+// recorded in mixed_run[node][a] (-1 when the region lies beyond the buffer:
+// the node pass then recomputes that corner).  Fixed regions need no shared
+// counter, so no atomic serialises the cells.
 template <int V>
 __device__ void emit_runs(const bm_params& P, const bm_buffers& B, const float (&vals)[V], int a, int f, int base,
-                          unsigned gmask) {
+                          unsigned gmask, int region) {
     const int s = threadIdx.x & 7;
-    const int lead = threadIdx.x & 24;
     int lo = f, hi = f == kMixed ? -1 : f;
     for (int d = 1; d < 8; d <<= 1) {
         lo = min(lo, __shfl_xor_sync(gmask, lo, d));
         hi = max(hi, __shfl_xor_sync(gmask, hi, d));
     }
     if (lo == hi) return;
-    int runs = 0;
-    for (int cur = lo; cur != kMixed;) {
-        ++runs;
-        int next = f > cur ? f : kMixed;
-        for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
-        cur = next;
-    }
-    int at = 0;
-    if (s == 0) at = atomicAdd(&B.flags[BM_FLAG_MIXED], runs);
-    at = __shfl_sync(gmask, at, lead);
+    const int at = region;
     const int node = base + node_offset(P, a);
-    const bool fits = at + runs <= P.mixed_capacity;
-    if (s == 0) B.mixed_run[node * 8 + a] = fits ? (at << 4) | runs : -1;
-    if (!fits) return;
+    if (at + 8 > P.mixed_capacity) {
+        if (s == 0) B.mixed_run[node * 8 + a] = -1;
+        return;
+    }
     int k = 0;
     for (int cur = lo; cur != kMixed; ++k) {
         float out[V];
@@ -331,6 +324,7 @@ __device__ void emit_runs(const bm_params& P, const bm_buffers& B, const float (
         for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
         cur = next;
     }
+    if (s == 0) B.mixed_run[node * 8 + a] = (at << 4) | k;
 }
 
 // Mixed-cell pass of p2g: 8 lanes per listed cell (warp-uniform loop).
@@ -372,7 +366,7 @@ __global__ void __launch_bounds__(256) k_p2g_mixed_cells(bm_params P, bm_buffers
                 vals[5] = k.J.y;
                 vals[6] = k.J.z;
             }
-            emit_runs<7>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask);
+            emit_runs<7>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask, (j * 8 + a) * 8);
         }
     }
 }
@@ -573,7 +567,6 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
 // partials of the MUSL re-scatter (material.py:400-401), thread (cell, slot).
 __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float half_skin, int check_list) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // runs of the re-scatter start over (p2g runs are consumed)
     const int cells = cell_count(P);
     const int c = t >> 3, s = t & 7;
     const int N = P.n, S = P.fmax * P.node_count, NC = P.node_count;
@@ -661,7 +654,7 @@ __global__ void __launch_bounds__(256) k_remap_mixed_cells(bm_params P, bm_buffe
                 vals[1] = r.y;
                 vals[2] = r.z;
             }
-            emit_runs<3>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask);
+            emit_runs<3>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask, (j * 8 + a) * 8);
         }
     }
 }
@@ -672,7 +665,6 @@ __global__ void __launch_bounds__(256) k_remap_mixed_cells(bm_params P, bm_buffe
 // single-field nodes; stores coupled / mass for the F update.
 __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) B.flags[BM_FLAG_MIXED] = 0;  // the next p2g's runs start over (re-scatter runs are read by k_remap_multi)
     if (t >= P.active_nodes) return;
     const int n = B.active[t];
     if (B.nfield[n] != 1) return;
@@ -934,12 +926,13 @@ __global__ void k_plastic_project(float* F, float* Fp, int n, float mu, float yi
 // must hold, neither has side effects), so the int64 division only runs for
 // particles in a knife's band.
 __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int cut_index, int cutting, bm_v3 xp,
-                             bm_v3 vp) {
+                             bm_v3 vp, unsigned knives) {
     if (cutting == 0) return;
     int64_t code = 0;
     bool loaded = false, changed = false;
     const float band = 6.0f * P.spacing;
     for (int k = 0; k < P.tool_count; ++k) {
+        if (((knives >> k) & 1u) == 0u) continue;
         const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
         const bm_v3 d = v3_sub(xp, T.edge);
         // cheap conservative band test on the knife axes (1 um beyond the exact bounds)
@@ -979,27 +972,61 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
     }
 }
 
+// Knives whose labelling band may hold some particle of this block (the same
+// mask in every thread): a knife is left out when the block's bounding box
+// lies beyond the per-particle band pre-test of assign_sides on the knife's
+// x or y axis, plus 1 um for rounding.
+__device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, bool active) {
+    __shared__ unsigned knives;
+    bm_v3 c, e;
+    float unused;
+    bool any;
+    block_box(x, 0.0f, active, &c, &e, &unused, &any);
+    if (threadIdx.x == 0) knives = 0u;
+    __syncthreads();
+    const int k = threadIdx.x;
+    if (any && k < P.tool_count) {
+        const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
+        const bm_v3 d = v3_sub(c, T.edge);
+        const bool out = fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) > 6.0f * P.spacing + 2.0e-6f ||
+                         fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + 2.0e-6f;
+        if (!out) atomicOr(&knives, 1u << k);
+    }
+    __syncthreads();
+    return knives;
+}
+
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
 // with this substep's side labelling (run after the tool update); thread 0
 // advances the substep counter of the friction-history ping-pong.
 __global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting, int advance_step) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
-    if (p >= P.n) return;
+    const bool active = p < P.n;
     const int N = P.n, S = P.fmax * P.node_count;
+    if (cutting) {
+        // the whole block takes part in the knife mask, so no thread leaves before it
+        const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero();
+        const unsigned knives = band_knives(P, B, xp, active);
+        if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, ld3(B.v, N, p), knives);
+    }
+    if (!active) return;
     if (do_update) {
         const int sid = B.stencil_id[p], base = B.base_node[p];
         const uint64_t fidx = B.fidx[p];
+        // update_F sums over slots with mass > 0.  The remap passes store a zero
+        // velocity in every registered slot without mass, and adding the (+-0)
+        // outer product of a zero velocity leaves the sum unchanged (it starts
+        // at +0 and never becomes -0), so all 8 corners are read unconditionally.
         bm_m33 rate = m33_zero();
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             const int s = slot_of(P, base, fidx, a);
-            if (B.grid_mass[s] > 0.0f) rate = m33_add(rate, m33_outer(ld3(B.remap_v, S, s), stencil_g(B, sid, a)));
+            rate = m33_add(rate, m33_outer(ld3(B.remap_v, S, s), stencil_g(B, sid, a)));
         }
         st9(B.F, N, p, m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt)));
         constitutive(P, B, p);
     }
-    if (cutting) assign_sides(P, B, p, cut_index, cutting, ld3(B.x, N, p), ld3(B.v, N, p));
 }
 
 // material.validate_interval (material.py:6-20).

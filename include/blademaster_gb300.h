@@ -132,7 +132,8 @@ typedef struct bm_buffers {
     float* cell_part;    /* [7][8][node_count] cell-corner partial sums: from the cell whose corner a is node n */
     uint8_t* cell_field; /* [node_count][8] field index of a uniform cell corner, 255 mixed, 254 no cell */
     int32_t* mixed_run;  /* [node_count][8] start << 4 | length of a mixed corner's per-field partials, -1 none */
-    float* mixed_part;   /* [mixed_capacity][8] per-field partials of mixed corners (7 sums, field as float) */
+    float* mixed_part;   /* [mixed_capacity][8] per-field partials of mixed corners (7 sums, field as float):
+                          * 8 entries for each corner of each listed mixed cell, (listed index * 8 + corner) * 8 */
     int32_t* multi_nodes;/* [active_nodes] nodes with more than one field */
     int32_t* mixed_cells;/* [cells] cells whose particles map to different fields at some corner */
     /* pair contact */
@@ -192,9 +193,10 @@ typedef struct bm_buffers {
 #define BM_FLAG_CHANGED 7        /* entries of buffers.changed */
 #define BM_FLAG_RELIST 8         /* entries of buffers.relist_list */
 #define BM_FLAG_MULTI 9          /* entries of buffers.multi_nodes */
-#define BM_FLAG_MIXED 10         /* entries of buffers.mixed_part in use */
+/* word 10 is unused */
 #define BM_FLAG_MIXED_CELLS 11   /* entries of buffers.mixed_cells */
 #define BM_FLAG_REGISTRATIONS 12 /* topology registrations run */
+#define BM_FLAG_MAX_DISP 13      /* float bits: largest |x - ref| at the last full pair-list build */
 #define BM_FLAG_WORDS 16
 
 typedef struct bm_solver bm_solver;
@@ -266,6 +268,8 @@ int bm_substeps(bm_solver* s, const bm_step_args* args, void* stream);
 int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_graph** out);
 int bm_graph_launch(bm_graph* g, void* stream);
 int bm_graph_destroy(bm_graph* g);
+/* Number of kernel launches one bm_graph_launch of `g` performs (its kernel nodes). */
+int bm_graph_kernel_count(const bm_graph* g, int64_t* count);
 /* Stages of one substep, in launch order (profiling). */
 #define BM_STAGE_PROLOGUE 0  /* clear_pair_slots + clear_step */
 #define BM_STAGE_RIGID 1     /* rigid_and_speed + extra_blade */
