@@ -259,39 +259,34 @@ __device__ __forceinline__ void warp_accumulate3(uint64_t* acc, bm_v3 v, bool an
     warp_accumulate(acc + 4, bm_fx_from_float(v.z));
 }
 
-// Knives that may be in contact with some particle of this block (the same
-// mask in every thread).  A knife is left out when, on one of its axes, the
-// block's bounding box lies farther from it than blade_at's per-particle axis
-// pre-test allows at the block's largest particle speed, plus 1 um for
-// rounding: every particle of the block then takes blade_at's "far" outcome.
-// Thread 0 also raises the substep's maximum particle speed (one atomic per
-// block; rigid_and_speed's atomic_max, contact.py:497).
+// Knives that may be in contact with some particle of this warp (the same
+// mask in every lane).  A knife is left out when, on one of its axes, the
+// warp's bounding box lies farther from it than blade_at's per-particle axis
+// pre-test allows at the warp's largest particle speed, plus 1 um for
+// rounding: every particle of the warp then takes blade_at's "far" outcome.
+// Lane 0 also raises the substep's maximum particle speed
+// (rigid_and_speed's atomic_max, contact.py:497).
 __device__ unsigned rigid_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, float speed, bool active,
                                  float radius_of_blade) {
-    __shared__ unsigned knives;
     bm_v3 c, e;
     float vmax;
     bool any;
-    block_box(x, speed, active, &c, &e, &vmax, &any);
-    if (threadIdx.x == 0) {
-        knives = 0u;
-        if (any) atomic_max_nonneg(B.speed, vmax);
-    }
-    __syncthreads();
-    const int k = threadIdx.x;
-    if (any && k < P.tool_count) {
+    warp_box(x, speed, active, &c, &e, &vmax, &any);
+    if (!any) return 0u;
+    const int k = threadIdx.x & 31;
+    if (k == 0) atomic_max_nonneg(B.speed, vmax);
+    bool near = false;
+    if (k < P.tool_count) {
         const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
         const float max_closing = (vmax + T.speed) + T.spin_reach;
         const float margin = (P.blade_offset + P.dt * max_closing) * 1.01f + 1.0e-6f;
         const float axis_margin = margin + 1.0e-5f * radius_of_blade + 1.0e-6f;
         const bm_v3 d = v3_sub(c, T.pos);
-        const bool far = fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) - P.half[0] > axis_margin ||
-                         fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) - P.half[1] > axis_margin ||
-                         fabsf(v3_dot(d, T.az)) - box_reach(T.az, e) - P.half[2] > axis_margin;
-        if (!far) atomicOr(&knives, 1u << k);
+        near = !(fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) - P.half[0] > axis_margin ||
+                 fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) - P.half[1] > axis_margin ||
+                 fabsf(v3_dot(d, T.az)) - box_reach(T.az, e) - P.half[2] > axis_margin);
     }
-    __syncthreads();
-    return knives;
+    return __ballot_sync(0xffffffffu, near);
 }
 
 // contact.rigid_and_speed + extra_blade (contact.py:422-566) for every knife.

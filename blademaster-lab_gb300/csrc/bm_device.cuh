@@ -86,15 +86,12 @@ __device__ __forceinline__ float blade_radius(const bm_params& P) {
     return sqrtf((P.half[0] * P.half[0] + P.half[1] * P.half[1]) + P.half[2] * P.half[2]);
 }
 
-// Bounding box (centre, half extent) of the positions of this block's active
-// particles and the largest of their `speed` values.  Every thread of the
-// block must call it, once per kernel; `*any` is false when the block has no
-// active particle.  The box is widened by 1 um so that it still contains
-// every position after the rounding of centre and extent.
-__device__ __forceinline__ void block_box(bm_v3 x, float speed, bool active, bm_v3* centre, bm_v3* extent,
-                                          float* max_speed, bool* any) {
-    __shared__ float warp_part[32][7];
-    __shared__ float box[7];
+// Bounding box (centre, half extent) of the positions of this warp's active
+// lanes and the largest of their `speed` values.  All 32 lanes must call;
+// `*any` is false when no lane is active.  The box is widened by 1 um so that
+// it still contains every position after the rounding of centre and extent.
+__device__ __forceinline__ void warp_box(bm_v3 x, float speed, bool active, bm_v3* centre, bm_v3* extent,
+                                         float* max_speed, bool* any) {
     const float inf = 3.0e38f;
     float v[7] = {active ? x.x : inf,  active ? x.y : inf,  active ? x.z : inf,   active ? -x.x : inf,
                   active ? -x.y : inf, active ? -x.z : inf, active ? -speed : inf};
@@ -102,22 +99,11 @@ __device__ __forceinline__ void block_box(bm_v3 x, float speed, bool active, bm_
     for (int i = 0; i < 7; ++i)
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) v[i] = fminf(v[i], __shfl_xor_sync(0xffffffffu, v[i], d));
-    const int warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
-    if ((threadIdx.x & 31) == 0)
-#pragma unroll
-        for (int i = 0; i < 7; ++i) warp_part[warp][i] = v[i];
-    __syncthreads();
-    if (threadIdx.x < 7) {
-        float m = inf;
-        for (int w = 0; w < warps; ++w) m = fminf(m, warp_part[w][threadIdx.x]);
-        box[threadIdx.x] = m;
-    }
-    __syncthreads();
-    *any = box[0] < inf;
-    const bm_v3 lo = v3(box[0], box[1], box[2]), hi = v3(-box[3], -box[4], -box[5]);
+    *any = v[0] < inf;
+    const bm_v3 lo = v3(v[0], v[1], v[2]), hi = v3(-v[3], -v[4], -v[5]);
     *centre = v3_mul(v3_add(lo, hi), 0.5f);
     *extent = v3_add(v3_mul(v3_sub(hi, lo), 0.5f), v3(1.0e-6f, 1.0e-6f, 1.0e-6f));
-    *max_speed = -box[6];
+    *max_speed = -v[6];
 }
 
 // Projection radius of a box with half extent e on direction a.

@@ -972,28 +972,25 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
     }
 }
 
-// Knives whose labelling band may hold some particle of this block (the same
-// mask in every thread): a knife is left out when the block's bounding box
-// lies beyond the per-particle band pre-test of assign_sides on the knife's
-// x or y axis, plus 1 um for rounding.
+// Knives whose labelling band may hold some particle of this warp (the same
+// mask in every lane): a knife is left out when the warp's bounding box lies
+// beyond the per-particle band pre-test of assign_sides on the knife's x or
+// y axis, plus 1 um for rounding.
 __device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, bool active) {
-    __shared__ unsigned knives;
     bm_v3 c, e;
     float unused;
     bool any;
-    block_box(x, 0.0f, active, &c, &e, &unused, &any);
-    if (threadIdx.x == 0) knives = 0u;
-    __syncthreads();
-    const int k = threadIdx.x;
-    if (any && k < P.tool_count) {
+    warp_box(x, 0.0f, active, &c, &e, &unused, &any);
+    if (!any) return 0u;
+    const int k = threadIdx.x & 31;
+    bool near = false;
+    if (k < P.tool_count) {
         const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
         const bm_v3 d = v3_sub(c, T.edge);
-        const bool out = fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) > 6.0f * P.spacing + 2.0e-6f ||
-                         fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + 2.0e-6f;
-        if (!out) atomicOr(&knives, 1u << k);
+        near = !(fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) > 6.0f * P.spacing + 2.0e-6f ||
+                 fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + 2.0e-6f);
     }
-    __syncthreads();
-    return knives;
+    return __ballot_sync(0xffffffffu, near);
 }
 
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
@@ -1005,7 +1002,7 @@ __global__ void k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int c
     const bool active = p < P.n;
     const int N = P.n, S = P.fmax * P.node_count;
     if (cutting) {
-        // the whole block takes part in the knife mask, so no thread leaves before it
+        // the whole warp takes part in the knife mask, so no lane leaves before it
         const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero();
         const unsigned knives = band_knives(P, B, xp, active);
         if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, ld3(B.v, N, p), knives);
