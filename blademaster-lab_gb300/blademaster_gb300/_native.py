@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_capi.cu", "bm_noalloc.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_capi.cu", "bm_noalloc.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -134,7 +134,8 @@ TOOL_F_WORDS = int(header_constant("BM_TOOL_F_WORDS"))
 FLAG = {
     k: int(header_constant("BM_FLAG_" + k))
     for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "CHANGED",
-              "RELIST", "MULTI", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "WORDS")
+              "RELIST", "MULTI", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "HOLD_NEEDS",
+              "HOLD_RESIDUAL", "HOLD_COUNT", "HOLD_NODES", "WORDS")
 }
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
 STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate"]
@@ -158,6 +159,7 @@ def _declare(lib):
         "bm_rigid_contacts": ([vp, i, vp], i),
         "bm_particle_contacts": ([vp, vp], i),
         "bm_particle_contacts_static": ([vp, vp], i),
+        "bm_hold_constraint": ([vp, vp], i),
         "bm_assign_sides": ([vp, i, i, vp], i),
         "bm_drive_tool": ([vp, i, vp], i),
         "bm_finish_external": ([vp, vp], i),

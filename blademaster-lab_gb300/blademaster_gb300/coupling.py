@@ -126,7 +126,7 @@ class ExternalToolPort:
         interval = s._t["interval"].cpu().numpy()
         self.timing_s["completion_and_readback"] += time.perf_counter() - readback_begin
         impulse, angular, errors = interval[:3].copy(), interval[3:6].copy(), out[6:9]
-        residual = 0.0
+        residual = s.blade_constraint.max_violation if s.blade_constraint is not None else 0.0
         if self.record_trajectory:
             self.trajectory = out[9 : 9 + 7 * samples].reshape(samples, 7)
             self.trajectory_times = np.linspace(0.0, duration_s, samples)

@@ -147,6 +147,27 @@ def _pow2_at_least(v):
     return 1 << (max(int(v), 1) - 1).bit_length()
 
 
+class BladeConstraint:
+    """Grid constraint of an externally held knife (blade_constraint.py:213-324).
+
+    Runs inside every substep of an external tool in hold mode; ``solve()``
+    runs it alone on the current grid velocities, as the reference's tests do.
+    ``max_violation`` is the largest final inward residual (m/s) of any solve
+    so far, which ExternalToolPort.advance checks against 1e-6 m/s.
+    """
+
+    def __init__(self, solver):
+        self.solver = solver
+
+    def solve(self):
+        self.solver._call("bm_hold_constraint", self.solver._stream)
+
+    @property
+    def max_violation(self):
+        bits = np.int32(self.solver._flag("HOLD_RESIDUAL"))
+        return float(bits.view(np.float32))
+
+
 class Solver:
     def __init__(self, config=Config(), device="cuda:0"):
         import torch
@@ -296,6 +317,16 @@ class Solver:
         T["rotations"][:, 3] = 1.0
         T["packed"] = zeros(49)
         T["result"] = zeros(10 + 7 * (MAX_BATCH + 1))
+        # held-blade constraint state (blade_constraint.py:213-240), sized only in hold mode
+        hold = cfg.external_tool and cfg.tool_substep == "hold"
+        nh, nc = (n, self.node_count) if hold else (1, 1)
+        T["hold"] = zeros(11, nh)
+        for name in ("hold_mark", "hold_pos", "hold_list"):
+            T[name] = zeros(nh, dtype=i32)
+        T["hold_entry"] = zeros(8 * nh, dtype=i32)
+        T["hold_node_start"] = zeros(nc + 1, dtype=i32)
+        T["hold_nodes"] = zeros(nc, dtype=i32)
+        T["hold_node_mark"] = zeros(nc, dtype=i32)
         self._t = T
         self._use_fp = bool(cfg.yield_stress > 0)
         self._params = self._make_params()
@@ -306,6 +337,7 @@ class Solver:
         self._bind()
         self._call("bm_sync_tool_mirror", self._stream)
         self._views()
+        self.blade_constraint = BladeConstraint(self) if hold else None
         self.field_codes = self.codes
         self.step_count = 0
         self.cut_index = 0

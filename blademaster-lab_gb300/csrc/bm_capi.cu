@@ -95,6 +95,7 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         bm::launch_register(s, field_codes, P.cache_topology ? 0 : 1, st);
         t.mark(4, st);
         bm::launch_material(s, 0, st);
+        if (P.external_tool && !P.predict) bm::launch_hold(s, st);
         t.mark(5, st);
         bm::launch_g2p(s, st);
         t.mark(6, st);
@@ -175,6 +176,12 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     for (const void* ptr : required)
         if (!ptr) return fail(BM_ERR_ARGUMENT, "a required buffer is null");
     if (P.maxwell && !buffers->viscous) return fail(BM_ERR_ARGUMENT, "maxwell requires the viscous buffer");
+    if (P.external_tool && !P.predict) {
+        const void* hold[] = {buffers->hold, buffers->hold_mark, buffers->hold_pos, buffers->hold_list,
+                              buffers->hold_entry, buffers->hold_node_start, buffers->hold_nodes, buffers->hold_node_mark};
+        for (const void* ptr : hold)
+            if (!ptr) return fail(BM_ERR_ARGUMENT, "hold mode requires the hold_* buffers");
+    }
     bm_solver* s = new (std::nothrow) bm_solver;
     if (!s) return fail(BM_ERR_STATE, "out of host memory");
     s->P = P;
@@ -220,10 +227,18 @@ int bm_material_step(bm_solver* s, int single_field, void* stream) {
     cudaStream_t st = as_stream(stream);
     bm::launch_register(s, single_field ? s->B.zero_codes : s->B.codes, s->P.cache_topology ? 0 : 1, st);
     bm::launch_material(s, 1, st);
+    if (s->P.external_tool && !s->P.predict) bm::launch_hold(s, st);
     bm::launch_g2p(s, st);
     bm::launch_remap(s, st);
     bm::launch_fupdate_assign(s, 1, 0, 0, 0, st);
     return check_cuda("material_step");
+}
+
+int bm_hold_constraint(bm_solver* s, void* stream) {
+    if (!s) return fail(BM_ERR_ARGUMENT, "null solver");
+    if (!s->P.external_tool || s->P.predict) return fail(BM_ERR_STATE, "the held-blade constraint needs an external tool in hold mode");
+    bm::launch_hold(s, as_stream(stream));
+    return check_cuda("hold_constraint");
 }
 
 int bm_rigid_contacts(bm_solver* s, int cut_bits, void* stream) {

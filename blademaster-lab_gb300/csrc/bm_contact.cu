@@ -871,6 +871,16 @@ void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) 
     k_pairs<<<gc, kBlock, 0, st>>>(P, B, reach);
 }
 
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, int32_t* total_out,
+                           const int32_t* gate, cudaStream_t st) {
+    const int64_t tiles = (count + 1023) / 1024;
+    const unsigned gt = tiles < 152 ? (unsigned)(tiles < 1 ? 1 : tiles) : 152;
+    const unsigned ga = grid_for(count) < 4 * 152 ? grid_for(count) : 4 * 152;
+    k_scan_tiles<<<gt, 1024, 0, st>>>(in, out, count, partials, gate);
+    k_scan_partials<<<1, 1024, 0, st>>>(partials, tiles, total_out, gate);
+    k_scan_add<<<ga, kBlock, 0, st>>>(out, count, partials, gate);
+}
+
 void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st) {
     if (reset) cudaMemsetAsync(&s->B.flags[BM_FLAG_EMBEDDED], 0, sizeof(int32_t), st);
     k_count_embedded<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B);

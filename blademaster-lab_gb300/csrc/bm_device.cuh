@@ -177,6 +177,24 @@ __device__ __forceinline__ void digit_masks(int64_t code, uint64_t* ones, uint64
     *twos = t;
 }
 
+// Visit the contributions to node n in ascending particle order: adjacent
+// cells in ascending cell index (stencil index a = 7 .. 0), particles of each
+// cell in order.  fn(p, a) is called for each.
+template <typename Fn>
+__device__ __forceinline__ void for_contributions(const bm_params& P, const bm_buffers& B, int n, Fn fn) {
+    const int nyz = P.node_dims[1] * P.node_dims[2];
+    const int i = n / nyz, j = (n / P.node_dims[2]) % P.node_dims[1], k = n % P.node_dims[2];
+#pragma unroll 1
+    for (int a = 7; a >= 0; --a) {
+        const int ci = i - ((a >> 2) & 1), cj = j - ((a >> 1) & 1), ck = k - (a & 1);
+        if (ci < 0 || cj < 0 || ck < 0 || ci >= P.cell_dims[0] || cj >= P.cell_dims[1] || ck >= P.cell_dims[2]) continue;
+        const int c = (ci * P.cell_dims[1] + cj) * P.cell_dims[2] + ck;
+        const int begin = B.cell_start[c], end = B.cell_start[c + 1];
+#pragma unroll 1
+        for (int p = begin; p < end; ++p) fn(p, a);
+    }
+}
+
 inline unsigned grid_for(int64_t count, int block = kBlock) {
     int64_t g = (count + block - 1) / block;
     return (unsigned)(g < 1 ? 1 : g);

@@ -38,6 +38,14 @@ void launch_pairs(const bm_solver* s, cudaStream_t st);
 // written before they are read) at `partials`.
 void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st);
 void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st);
+// Exclusive prefix sum of `count` ints (one int of `partials` per 1024 of
+// them); the total goes to *total_out.  Every kernel returns at once when
+// `gate` is non-null and *gate == 0.
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, int32_t* total_out,
+                           const int32_t* gate, cudaStream_t st);
+
+// held-blade constraint (external tool in hold mode)
+void launch_hold(const bm_solver* s, cudaStream_t st);
 void launch_blade_query(const float* local, int n, const float* half, float bevel, float* closest, float* normal,
                         float* distance, cudaStream_t st);
 void launch_friction(const float* normal, const float* relative, const float* jn, const float* history, int n, float me,

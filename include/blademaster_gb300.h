@@ -173,6 +173,15 @@ typedef struct bm_buffers {
     float* packed;       /* [49] external tool state */
     float* result;       /* [10 + 7 * samples] interval result */
     int32_t* scratch;    /* [scratch_len] scan workspace */
+    /* held-blade grid constraint (external tool with tool_substep "hold" only; may be null otherwise) */
+    float* hold;         /* [11][n]: entry side, normal xyz, lever xyz, rhs, row bound, impulse, extrapolated */
+    int32_t* hold_mark;  /* [n] 1 if the particle is a constraint contact this substep */
+    int32_t* hold_pos;   /* [n] exclusive prefix sum of hold_mark */
+    int32_t* hold_list;  /* [n] contacts in ascending particle order */
+    int32_t* hold_entry; /* [8 n] contacts at each listed node, particle << 3 | corner, ascending particle */
+    int32_t* hold_node_start; /* [node_count + 1] */
+    int32_t* hold_nodes; /* [node_count] grid nodes the contacts touch */
+    int32_t* hold_node_mark; /* [node_count] all zero between substeps */
 } bm_buffers;
 
 /* Layout of buffers.acc: pairs of uint64 (lo, hi), 2^-96 fixed point. */
@@ -197,7 +206,11 @@ typedef struct bm_buffers {
 #define BM_FLAG_MIXED_CELLS 11   /* entries of buffers.mixed_cells */
 #define BM_FLAG_REGISTRATIONS 12 /* topology registrations run */
 #define BM_FLAG_MAX_DISP 13      /* float bits: largest |x - ref| at the last full pair-list build */
-#define BM_FLAG_WORDS 16
+#define BM_FLAG_HOLD_NEEDS 14    /* held-blade constraint: some contact violates this substep */
+#define BM_FLAG_HOLD_RESIDUAL 15 /* float bits: largest final residual (m/s) of any constraint solve so far */
+#define BM_FLAG_HOLD_COUNT 16    /* held-blade constraint: contacts this substep */
+#define BM_FLAG_HOLD_NODES 17    /* held-blade constraint: grid nodes the contacts touch */
+#define BM_FLAG_WORDS 24
 
 typedef struct bm_solver bm_solver;
 typedef struct bm_graph bm_graph;
@@ -240,6 +253,11 @@ int bm_material_step(bm_solver* s, int single_field, void* stream);
 int bm_rigid_contacts(bm_solver* s, int cut_bits, void* stream);
 /* Solver.particle_contacts (solver.py:670-751): pair contact with friction history. */
 int bm_particle_contacts(bm_solver* s, void* stream);
+/* BladeConstraint.solve (blade_constraint.py:254-324) for the externally held
+ * knife 0 on the current grid velocities: the projected-gradient solve of the
+ * broad-face contacts, its grid velocity correction and reaction.  Part of
+ * every substep of an external tool in hold mode; exposed for tests. */
+int bm_hold_constraint(bm_solver* s, void* stream);
 /* bm_particle_contacts with the bucket-scan workspace of the pair-list rebuild
  * in a static device array of BM_STATIC_SCAN_PARTIALS ints (64 KiB) instead of
  * buffers.scratch; it allocates nothing.  No counterpart in the reference: it

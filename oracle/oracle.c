@@ -87,6 +87,7 @@ typedef struct orc_state {
     int32_t* errors;       /* [3] */
     int32_t* flags;        /* BM_FLAG_WORDS */
     float* result;         /* [10 + 7 * samples] */
+    float* hold_side;      /* [n] entry side of each particle at the held knife (-1, 0, +1) */
     int64_t capacity;      /* key table capacity */
     int64_t buckets;       /* pair search buckets (power of two) */
 } orc_state;
@@ -570,6 +571,170 @@ static void update_F(const bm_params* P, orc_state* S, int64_t p) {
 }
 
 /* Solver.material_step (solver.py:334-376) and _material_transfers (431-535). */
+/* ------------------------------------------------ held-blade constraint */
+
+/* Per-slot scatter of w * j_p over the particles with `active` set, for the
+ * slots of the listed nodes, then couple (couple_at, material.py:155-179)
+ * into C; both zeroed first for those slots.  Order of a slot's sum: the
+ * adjacent cells in ascending cell index (corner a = 7 ... 0), within a cell
+ * ascending particles; one sequential float sum. */
+static void hold_scatter_couple(const bm_params* P, orc_state* S, const int64_t* nodes, int64_t node_total,
+                                const char* active, const float* j, float* G, float* C) {
+    int64_t t;
+    for (t = 0; t < node_total; ++t) {
+        int64_t X = nodes[t], i;
+        int a;
+        for (i = S->node_start[X]; i < S->node_start[X + 1]; ++i) {
+            int64_t s = S->node_slots[i];
+            bm_v3 g = v3_zero();
+            for (a = 7; a >= 0; --a) {
+                int64_t c = cell_at(P, X, a), p;
+                if (c < 0) continue;
+                for (p = S->cell_start[c]; p < S->cell_start[c + 1]; ++p)
+                    if (active[p] && S->slots[8 * p + a] == s) g = v3_add(g, v3_mul(ld3(j, p), S->weights[8 * p + a]));
+            }
+            st3(G, s, g);
+        }
+        for (i = S->node_start[X]; i < S->node_start[X + 1]; ++i) {
+            int64_t s = S->node_slots[i];
+            st3(C, s, v3_zero());
+            couple(P, S, G, C, s);
+        }
+    }
+}
+
+/* response_at (blade_constraint.py:114-127): sum over a of w C / m, mass > 0. */
+static bm_v3 hold_response(const orc_state* S, int64_t p, const float* C) {
+    bm_v3 r = v3_zero();
+    int a;
+    for (a = 0; a < 8; ++a) {
+        int32_t s = S->slots[8 * p + a];
+        if (s >= 0 && S->grid_mass[s] > 0.0f) r = v3_add(r, v3_div(v3_mul(ld3(C, s), S->weights[8 * p + a]), S->grid_mass[s]));
+    }
+    return r;
+}
+
+/* BladeConstraint.solve (blade_constraint.py:254-324) for the externally held
+ * knife 0: prepare (13-70), row_bound (73-90), batches of 48 projected
+ * gradient iterations (project 130-152) until the largest inward residual
+ * (record_residual 155-168) is at most 1e-6 m/s or 8 batches ran
+ * (finish_refinement 171-184), then apply_grid (187-194) and apply_reaction
+ * (197-205).  The reaction is subtracted in the exact fixed-point sums. */
+static void hold_constraint(const bm_params* P, orc_state* S) {
+    int64_t n = P->n, cap = S->capacity, p, m = 0, node_total = 0, t;
+    tool_f32 T = tool_mirror(S->tool);
+    float *normal = (float*)calloc((size_t)(3 * n), sizeof(float)), *lever = (float*)calloc((size_t)(3 * n), sizeof(float));
+    float *rhs = (float*)calloc((size_t)n, sizeof(float)), *bound = (float*)calloc((size_t)n, sizeof(float));
+    float *imp = (float*)calloc((size_t)n, sizeof(float)), *ext = (float*)calloc((size_t)n, sizeof(float));
+    float *j = (float*)calloc((size_t)(3 * n), sizeof(float));
+    float *G = (float*)calloc((size_t)(3 * cap), sizeof(float)), *C = (float*)calloc((size_t)(3 * cap), sizeof(float));
+    char *active = (char*)calloc((size_t)n, 1), *mark = (char*)calloc((size_t)P->node_count, 1);
+    int64_t *list = (int64_t*)malloc(sizeof(int64_t) * (size_t)n), *nodes = NULL;
+    int needs = 0, batches = 0, a;
+    float residual = 0.0f;
+    for (p = 0; p < n; ++p) {
+        bm_v3 local = q_rotate_inv(T.rot, v3_sub(ld3(S->x, p), T.pos)), grid_v = v3_zero(), nn, g;
+        float side, gap;
+        if (fabsf(local.y) >= P->half[1] || local.z <= -P->half[2] + P->bevel || local.z >= P->half[2]) {
+            S->hold_side[p] = 0.0f;
+            continue;
+        }
+        for (a = 0; a < 8; ++a) grid_v = v3_add(grid_v, v3_mul(ld3(S->new_v, S->slots[8 * p + a]), S->weights[8 * p + a]));
+        side = S->hold_side[p];
+        if (side == 0.0f || fabsf(local.x) > P->half[0] + P->blade_offset) side = local.x < 0.0f ? -1.0f : 1.0f;
+        nn = q_rotate(T.rot, v3(side, 0.0f, 0.0f));
+        gap = side * local.x - P->half[0];
+        if (gap > P->blade_offset && gap + P->dt * v3_dot(grid_v, nn) > 0.0f) {
+            S->hold_side[p] = 0.0f;
+            continue;
+        }
+        S->hold_side[p] = side;
+        active[p] = 1;
+        st3(normal, p, nn);
+        st3(lever, p, q_rotate(T.rot, v3(side * P->half[0], local.y, local.z)));
+        rhs[p] = -bm_maxf(gap, 0.0f) / P->dt - v3_dot(grid_v, nn);
+        if (rhs[p] > 1.0e-7f) needs = 1;
+    }
+    if (needs) {
+        for (p = 0; p < n; ++p)
+            if (active[p]) {
+                list[m++] = p;
+                for (a = 0; a < 8; ++a) mark[S->nodes[8 * p + a]] = 1;
+            }
+        nodes = (int64_t*)malloc(sizeof(int64_t) * (size_t)P->node_count);
+        for (t = 0; t < P->node_count; ++t)
+            if (mark[t]) nodes[node_total++] = t;
+        /* active weights (w, 0, 0) coupled, then the absolute row-sum bound */
+        for (t = 0; t < m; ++t) st3(j, list[t], v3(1.0f, 0.0f, 0.0f));
+        hold_scatter_couple(P, S, nodes, node_total, active, j, G, C);
+        for (t = 0; t < m; ++t) {
+            float total = 0.0f;
+            p = list[t];
+            for (a = 0; a < 8; ++a) {
+                int32_t s = S->slots[8 * p + a];
+                if (s >= 0 && S->grid_mass[s] > 0.0f) total = total + S->weights[8 * p + a] * C[3 * s] / S->grid_mass[s];
+            }
+            bound[p] = total;
+        }
+        for (;;) {
+            int it;
+            for (t = 0; t < m; ++t) ext[list[t]] = imp[list[t]];
+            for (it = 0; it < 48; ++it) {
+                float acc = (float)((double)it / (double)(it + 3));
+                for (t = 0; t < m; ++t) st3(j, list[t], v3_mul(ld3(normal, list[t]), ext[list[t]]));
+                hold_scatter_couple(P, S, nodes, node_total, active, j, G, C);
+                for (t = 0; t < m; ++t) {
+                    bm_v3 r;
+                    float previous, current;
+                    p = list[t];
+                    r = hold_response(S, p, C);
+                    previous = imp[p];
+                    current = bm_maxf(0.0f, ext[p] + (rhs[p] - v3_dot(ld3(normal, p), r)) / bm_maxf(bound[p], 1.0e-12f));
+                    imp[p] = current;
+                    ext[p] = current + acc * (current - previous);
+                }
+            }
+            for (t = 0; t < m; ++t) st3(j, list[t], v3_mul(ld3(normal, list[t]), imp[list[t]]));
+            hold_scatter_couple(P, S, nodes, node_total, active, j, G, C);
+            residual = 0.0f;
+            for (t = 0; t < m; ++t) {
+                p = list[t];
+                residual = bm_maxf(residual, bm_maxf(0.0f, rhs[p] - v3_dot(ld3(normal, p), hold_response(S, p, C))));
+            }
+            batches += 1;
+            if (!(residual > 1.0e-6f && batches < 8)) break;
+        }
+        {
+            float previous = bm_u2f((uint32_t)S->flags[BM_FLAG_HOLD_RESIDUAL]);
+            S->flags[BM_FLAG_HOLD_RESIDUAL] = (int32_t)bm_f2u(bm_maxf(previous, residual));
+        }
+        /* apply_grid: every slot with mass (C is zero away from the contacts) */
+        for (t = 0; t < cap; ++t)
+            if (S->keys[t] >= 0 && S->grid_mass[t] > 0.0f)
+                st3(S->new_v, t, v3_add(ld3(S->new_v, t), v3_div(ld3(C, t), S->grid_mass[t])));
+        /* apply_reaction: reaction -= sum j, torque -= sum lever x j */
+        {
+            bm_fx sums[6];
+            int k;
+            for (k = 0; k < 6; ++k) sums[k] = acc_get(S->acc, k < 3 ? BM_ACC_REACTION(0) + 2 * k : BM_ACC_TORQUE(0) + 2 * (k - 3));
+            for (t = 0; t < m; ++t) {
+                bm_v3 jj = ld3(j, list[t]), tq = v3_cross(ld3(lever, list[t]), jj);
+                sums[0] = bm_fx_add(sums[0], bm_fx_from_float(-jj.x));
+                sums[1] = bm_fx_add(sums[1], bm_fx_from_float(-jj.y));
+                sums[2] = bm_fx_add(sums[2], bm_fx_from_float(-jj.z));
+                sums[3] = bm_fx_add(sums[3], bm_fx_from_float(-tq.x));
+                sums[4] = bm_fx_add(sums[4], bm_fx_from_float(-tq.y));
+                sums[5] = bm_fx_add(sums[5], bm_fx_from_float(-tq.z));
+            }
+            for (k = 0; k < 6; ++k) acc_put(S->acc, k < 3 ? BM_ACC_REACTION(0) + 2 * k : BM_ACC_TORQUE(0) + 2 * (k - 3), sums[k]);
+        }
+        S->flags[BM_FLAG_HOLD_COUNT] = (int32_t)m;
+        S->flags[BM_FLAG_HOLD_NODES] = (int32_t)node_total;
+    }
+    free(normal); free(lever); free(rhs); free(bound); free(imp); free(ext); free(j); free(G); free(C);
+    free(active); free(mark); free(list); free(nodes);
+}
+
 ORC_API void orc_material_step(const bm_params* P, orc_state* S, const int64_t* field_codes, int register_now) {
     int64_t s, p;
     if (register_now) orc_register(P, S, field_codes);
@@ -589,6 +754,7 @@ ORC_API void orc_material_step(const bm_params* P, orc_state* S, const int64_t* 
 #pragma omp parallel for schedule(static)
         for (s = 0; s < S->capacity; ++s) couple_and_velocity(P, S, s);
     }
+    if (P->external_tool && !P->predict) hold_constraint(P, S);
 #pragma omp parallel for schedule(static)
     for (p = 0; p < P->n; ++p) g2p_at(P, S, p);
     remap(P, S);

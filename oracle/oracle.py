@@ -60,7 +60,7 @@ _STATE_FIELDS = [
     "weights", "gradients", "keys", "slots", "node_start", "node_slots", "slot_start", "contrib", "grid_mass",
     "momentum", "grid_impulse", "old_v", "new_v", "remapped", "coupled", "pair_keys", "pair_history", "pair_used",
     "pair_count", "cell_head", "cell_start", "cell_next", "tool", "mobility", "acc", "interval", "table_impulse", "speed",
-    "errors", "flags", "result",
+    "errors", "flags", "result", "hold_side",
 ]
 
 
@@ -249,6 +249,7 @@ class OracleSolver:
         A["flags"] = np.zeros(_native.FLAG["WORDS"], np.int32)
         A["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
         A["result"] = np.zeros(10 + 7 * 4097, np.float32)
+        A["hold_side"] = np.zeros(n, np.float32)
         s = State()
         for name in _STATE_FIELDS:
             setattr(s, name, A[name].ctypes.data)
@@ -268,6 +269,8 @@ class OracleSolver:
             return A[name][self.rank]
         if name in ("F", "Fp", "stress"):
             return A[name][self.rank].reshape(-1, 3, 3)
+        if name == "hold_side":
+            return A["hold_side"][self.rank]
         if name in ("codes", "damage"):
             return A[name][self.rank] if name == "codes" else A["damage"][0][self.rank]
         if name == "tool_damage":
