@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_capi.cu", "bm_noalloc.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_capi.cu", "bm_noalloc.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -122,6 +122,14 @@ class StepArgs(ctypes.Structure):
     _fields_ = _struct_fields("bm_step_args")
 
 
+class MlsParams(ctypes.Structure):
+    _fields_ = _struct_fields("bm_mls_params")
+
+
+class MlsBuffers(ctypes.Structure):
+    _fields_ = _struct_fields("bm_mls_buffers")
+
+
 def header_constant(name):
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
     m = re.search(r"#define %s \(?([^\n]+)" % name, text)
@@ -160,6 +168,11 @@ def _declare(lib):
         "bm_particle_contacts": ([vp, vp], i),
         "bm_particle_contacts_static": ([vp, vp], i),
         "bm_hold_constraint": ([vp, vp], i),
+        "bm_mls_create": ([ctypes.POINTER(MlsParams), ctypes.POINTER(MlsBuffers), ctypes.POINTER(Params),
+                           ctypes.POINTER(Buffers), ctypes.POINTER(vp)], i),
+        "bm_mls_destroy": ([vp], i),
+        "bm_mls_substeps": ([vp, i, vp], i),
+        "bm_mls_graph_create": ([vp, i, vp, ctypes.POINTER(vp)], i),
         "bm_assign_sides": ([vp, i, i, vp], i),
         "bm_drive_tool": ([vp, i, vp], i),
         "bm_finish_external": ([vp, vp], i),

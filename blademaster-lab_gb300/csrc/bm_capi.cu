@@ -126,10 +126,6 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
 
 }  // namespace
 
-struct bm_graph {
-    cudaGraph_t graph;
-    cudaGraphExec_t exec;
-};
 
 extern "C" {
 

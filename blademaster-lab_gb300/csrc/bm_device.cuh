@@ -143,6 +143,27 @@ __device__ __forceinline__ bm_fx fx_zero() {
     return z;
 }
 
+// 128-bit accumulator triples and float64 vectors in plain arrays.
+__device__ __forceinline__ bm_v3d acc_read3(const uint64_t* acc, int word) {
+    bm_fx a, b, c;
+    a.lo = acc[word];
+    a.hi = acc[word + 1];
+    b.lo = acc[word + 2];
+    b.hi = acc[word + 3];
+    c.lo = acc[word + 4];
+    c.hi = acc[word + 5];
+    return v3d(bm_fx_to_double(a), bm_fx_to_double(b), bm_fx_to_double(c));
+}
+__device__ __forceinline__ void acc_clear3(uint64_t* acc, int word) {
+    for (int i = 0; i < 6; ++i) acc[word + i] = 0u;
+}
+__device__ __forceinline__ bm_v3d dget3(const double* t) { return v3d(t[0], t[1], t[2]); }
+__device__ __forceinline__ void dput3(double* t, bm_v3d v) {
+    t[0] = v.x;
+    t[1] = v.y;
+    t[2] = v.z;
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(float* addr, float v) {
     // Non-negative floats order like their bit patterns.
     atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
@@ -193,6 +214,18 @@ __device__ __forceinline__ void for_contributions(const bm_params& P, const bm_b
 #pragma unroll 1
         for (int p = begin; p < end; ++p) fn(p, a);
     }
+}
+
+// material.corotated_stress (material.py:78-91) from the SVD of F Fp^-1.
+__device__ __forceinline__ bm_m33 corotated_svd(const bm_m33& U, bm_v3 s, const bm_m33& V, const bm_m33& plastic_inverse, float mu,
+                                float lam) {
+    const float J = (s.x * s.y) * s.z;
+    bm_v3 d;
+    for (int i = 0; i < 3; ++i) {
+        const float si = v3_get(s, i);
+        v3_set(&d, i, 2.0f * mu * (si - 1.0f) + lam * (J - 1.0f) * J / si);
+    }
+    return m33_mul(m33_mul(m33_mul(U, m33_diag(d)), m33_transpose(V)), m33_transpose(plastic_inverse));
 }
 
 inline unsigned grid_for(int64_t count, int block = kBlock) {

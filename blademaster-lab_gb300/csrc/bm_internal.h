@@ -16,6 +16,11 @@ struct bm_solver {
     cudaEvent_t fork, join;
 };
 
+struct bm_graph {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
 namespace bm {
 
 // material

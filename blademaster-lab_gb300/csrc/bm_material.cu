@@ -741,17 +741,6 @@ __device__ __forceinline__ bm_m33 corotated_polar(const bm_m33& f, float J, floa
     return out;
 }
 
-__device__ bm_m33 corotated_svd(const bm_m33& U, bm_v3 s, const bm_m33& V, const bm_m33& plastic_inverse, float mu,
-                                float lam) {
-    const float J = (s.x * s.y) * s.z;
-    bm_v3 d;
-    for (int i = 0; i < 3; ++i) {
-        const float si = v3_get(s, i);
-        v3_set(&d, i, 2.0f * mu * (si - 1.0f) + lam * (J - 1.0f) * J / si);
-    }
-    return m33_mul(m33_mul(m33_mul(U, m33_diag(d)), m33_transpose(V)), m33_transpose(plastic_inverse));
-}
-
 // material.stress_at (material.py:94-112).
 __device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
     const int N = P.n;

@@ -491,6 +491,31 @@ BM_HD bm_fx bm_fx_add(bm_fx a, bm_fx b) {
     return r;
 }
 /* Exact for |f| >= 2^-73; smaller magnitudes round half away from zero; |f| < 2^31 required. */
+/* f * 2^k rounded to the nearest integer (halves away from zero) as int64,
+ * from the float's bits so that CPU and GPU agree; |result| saturates at
+ * 2^62 and non-finite f gives 0.  Sums of such values are exact and do not
+ * depend on their order. */
+BM_HD int64_t bm_fixed64(float f, int k) {
+    uint32_t bits = bm_f2u(f);
+    int exponent = (int)((bits >> 23) & 0xffu), shift;
+    uint64_t mant = bits & 0x007fffffu, mag;
+    if (exponent == 0xff) return 0;
+    if (exponent == 0) exponent = 1; else mant |= 0x00800000u;
+    if (mant == 0u) return 0;
+    /* |f| = mant * 2^(exponent - 150) */
+    shift = exponent - 150 + k;
+    if (shift >= 0) {
+        mag = shift > 38 ? ((uint64_t)1 << 62) : (mant << shift);
+    } else {
+        int down = -shift;
+        if (down > 25) return 0;
+        mag = (mant + ((uint64_t)1 << (down - 1))) >> down;
+    }
+    return (bits >> 31) ? -(int64_t)mag : (int64_t)mag;
+}
+/* The float nearest to v * 2^-k (one rounding; 2^-k is applied exactly). */
+BM_HD float bm_unfixed64(int64_t v, int k) { return (float)v * bm_u2f((uint32_t)(127 - k) << 23); }
+
 BM_HD bm_fx bm_fx_from_float(float f) {
     uint32_t bits = bm_f2u(f);
     int exponent = (int)((bits >> 23) & 0xffu);

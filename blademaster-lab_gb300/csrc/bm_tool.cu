@@ -6,26 +6,6 @@
 
 namespace bm {
 
-__device__ __forceinline__ bm_v3d acc_read3(const uint64_t* acc, int word) {
-    bm_fx a, b, c;
-    a.lo = acc[word];
-    a.hi = acc[word + 1];
-    b.lo = acc[word + 2];
-    b.hi = acc[word + 3];
-    c.lo = acc[word + 4];
-    c.hi = acc[word + 5];
-    return v3d(bm_fx_to_double(a), bm_fx_to_double(b), bm_fx_to_double(c));
-}
-__device__ __forceinline__ void acc_clear3(uint64_t* acc, int word) {
-    for (int i = 0; i < 6; ++i) acc[word + i] = 0u;
-}
-__device__ __forceinline__ bm_v3d dget3(const double* t) { return v3d(t[0], t[1], t[2]); }
-__device__ __forceinline__ void dput3(double* t, bm_v3d v) {
-    t[0] = v.x;
-    t[1] = v.y;
-    t[2] = v.z;
-}
-
 // Float32 knife record read by the particle kernels; the derived entries are
 // evaluated with the same operations the particle code would apply.
 __device__ void write_mirror(const bm_params& P, const bm_buffers& B, int k) {

@@ -342,6 +342,58 @@ int bm_resist_cut_probe(const float* j, const float* x, const float* v, const fl
 /* material.plastic_project (material.py:434-442) on [9][n] F and Fp. */
 int bm_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, void* stream);
 
+/* ------------------------------------------------------------------------
+ * MLS-MPM cutting baseline (blademaster_warp/mlsmpm.py): updated-Lagrangian
+ * MLS-MPM with quadratic B-splines, APIC transfer and one velocity field on
+ * a dense grid, TopoCut damage (Eqs. 6-7), and the same rigid contact as the
+ * TLMPM solver with knife 0 held (tool model -1, zero mobility).  Particles
+ * stay in the reference order.  Grid sums are exact 64-bit fixed point
+ * (value * 2^shift), so they do not depend on the order of the scatter.
+ * ------------------------------------------------------------------------ */
+typedef struct bm_mls_params {
+    int32_t n;
+    int32_t dims[3];          /* dense grid nodes per axis */
+    int32_t plastic;          /* yield_stress > 0: Hencky return map with softening */
+    int32_t mass_shift;       /* grid mass fixed point: value * 2^mass_shift */
+    int32_t momentum_shift;   /* grid momentum fixed point: value * 2^momentum_shift */
+    int32_t pad;
+    float origin[3];          /* position of grid node (0, 0, 0) */
+    float dx, dt, mass, volume, mu, lam;
+    float damaged_shear;      /* shear modulus factor of damaged particles */
+    float softening;          /* Eq. 7 gamma, Pa per unit plastic strain */
+    float compressed, stretched; /* Eq. 6 J bounds */
+} bm_mls_params;
+
+typedef struct bm_mls_buffers {
+    float* x;                 /* [3][n] reference particle order */
+    float* v;                 /* [3][n] */
+    float* C;                 /* [9][n] APIC affine velocity, row-major */
+    float* F;                 /* [9][n] */
+    float* yield_stress;      /* [n] */
+    float* damage;            /* [n] */
+    float* damage_reference;  /* [n] J of the Eq. 6 reference state, 0 while damage is off */
+    int64_t* grid_mass;       /* [nodes] fixed point */
+    int64_t* grid_momentum;   /* [3][nodes] fixed point */
+    float* grid_v;            /* [3][nodes] */
+    int32_t* inversions;      /* [1] particle-steps with det F <= 0 before the clamp */
+} bm_mls_buffers;
+
+typedef struct bm_mls bm_mls;
+
+/* MlsSolver.__init__ (mlsmpm.py:232-291).  `contact` and `contact_buffers`
+ * describe the rigid contact exactly as for bm_solver_create (n and the
+ * particle arrays x, v shared with `buffers`; one tool; histories [2][3][n],
+ * hist_mask, damage [n] unused, impulses [3][n], tool, tool_f, mobility, acc,
+ * interval, speed, errors, flags, packed, result). */
+int bm_mls_create(const bm_mls_params* params, const bm_mls_buffers* buffers, const bm_params* contact,
+                  const bm_buffers* contact_buffers, bm_mls** out);
+int bm_mls_destroy(bm_mls* s);
+/* `steps` substeps (MlsSolver._substep, mlsmpm.py:293-393) after loading the
+ * knife state from contact_buffers.packed (load_external_state). */
+int bm_mls_substeps(bm_mls* s, int steps, void* stream);
+/* The same interval captured as a CUDA graph (MlsSolver.advance, mlsmpm.py:395-426). */
+int bm_mls_graph_create(bm_mls* s, int steps, void* stream, bm_graph** out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1455,6 +1455,174 @@ ORC_API void orc_substep(const bm_params* P, orc_state* S, int cut_bits, int cut
     S->flags[BM_FLAG_STEP] += 1;
 }
 
+/* --------------------------------------------------------------- MLS-MPM */
+
+/* MlsSolver state (mlsmpm.py:232-291), particle arrays AoS in reference order. */
+typedef struct {
+    float* x;                /* [n][3] (shared with the contact state) */
+    float* v;                /* [n][3] */
+    float* C;                /* [n][9] */
+    float* F;                /* [n][9] */
+    float* yield_stress;     /* [n] */
+    float* damage;           /* [n] */
+    float* damage_reference; /* [n] */
+    int64_t* grid_mass;      /* [nodes] fixed point */
+    int64_t* grid_momentum;  /* [nodes][3] fixed point */
+    float* grid_v;           /* [nodes][3] */
+    int32_t* inversions;     /* [1] */
+} orc_mls_state;
+
+ORC_API uint32_t orc_mls_state_size(void) { return (uint32_t)sizeof(orc_mls_state); }
+
+/* spline_weights (mlsmpm.py:41-51). */
+static void mls_weights(bm_v3 fx, float w[3][3]) {
+    int axis;
+    for (axis = 0; axis < 3; ++axis) {
+        float f = v3_get(fx, axis);
+        w[0][axis] = 0.5f * (1.5f - f) * (1.5f - f);
+        w[1][axis] = 0.75f - (f - 1.0f) * (f - 1.0f);
+        w[2][axis] = 0.5f * (f - 0.5f) * (f - 0.5f);
+    }
+}
+
+/* cell_base + inside_domain (mlsmpm.py:54-72). */
+static int mls_locate(const bm_mls_params* M, bm_v3 x, int base[3], bm_v3* fx) {
+    bm_v3 local;
+    float f[3];
+    int i;
+    if (!bm_isfinitef(x.x) || !bm_isfinitef(x.y) || !bm_isfinitef(x.z)) return 0;
+    local = v3_div(v3_sub(x, v3(M->origin[0], M->origin[1], M->origin[2])), M->dx);
+    for (i = 0; i < 3; ++i) {
+        float b = floorf(v3_get(local, i) - 0.5f);
+        if (!(b >= 0.0f && b < (float)(M->dims[i] - 2))) return 0;
+        base[i] = (int)b;
+        f[i] = v3_get(local, i) - b;
+    }
+    *fx = v3(f[0], f[1], f[2]);
+    return 1;
+}
+
+/* MlsSolver._substep (mlsmpm.py:293-393): rigid_and_speed for the held knife
+ * (cutting off), accumulate_reaction, p2g (exact fixed-point grid sums),
+ * grid_update, g2p. */
+ORC_API void orc_mls_substep(const bm_mls_params* M, orc_mls_state* T, const bm_params* P, orc_state* S) {
+    int64_t n = M->n, nodes = (int64_t)M->dims[0] * M->dims[1] * M->dims[2], p, node;
+    int32_t inversions = 0;
+    orc_rigid_contacts(P, S, 0);
+    {
+        bm_v3d j = acc_read3(S->acc, BM_ACC_REACTION(0)), tau = acc_read3(S->acc, BM_ACC_TORQUE(0));
+        S->interval[0] += j.x; S->interval[1] += j.y; S->interval[2] += j.z;
+        S->interval[3] += tau.x; S->interval[4] += tau.y; S->interval[5] += tau.z;
+        acc_clear3(S->acc, BM_ACC_REACTION(0));
+        acc_clear3(S->acc, BM_ACC_TORQUE(0));
+        acc_clear3(S->acc, BM_ACC_BOARD);
+        S->speed[0] = 0.0f;
+    }
+    memset(T->grid_mass, 0, sizeof(int64_t) * (size_t)nodes);
+    memset(T->grid_momentum, 0, sizeof(int64_t) * 3 * (size_t)nodes);
+#pragma omp parallel for schedule(static)
+    for (p = 0; p < n; ++p) {
+        int base[3], i, j, k;
+        bm_v3 fx, sigma, momentum;
+        float w[3][3], shear;
+        bm_m33 F, U, V, Ps, stress, affine;
+        if (!mls_locate(M, ld3(T->x, p), base, &fx)) continue;
+        mls_weights(fx, w);
+        shear = T->damage[p] > 0.0f ? M->mu * M->damaged_shear : M->mu;
+        F = ld9(T->F, p);
+        bm_svd3(F, &U, &sigma, &V);
+        Ps = corotated_stress(U, sigma, V, m33_identity(), shear, M->lam);
+        stress = m33_mul(m33_scale(Ps, (-M->dt * M->volume * 4.0f) / (M->dx * M->dx)), m33_transpose(F));
+        affine = m33_add(stress, m33_scale(ld9(T->C, p), M->mass));
+        momentum = v3_add(v3_mul(ld3(T->v, p), M->mass), ld3(S->impulses, p));
+        for (i = 0; i < 3; ++i)
+            for (j = 0; j < 3; ++j)
+                for (k = 0; k < 3; ++k) {
+                    float weight = (w[i][0] * w[j][1]) * w[k][2];
+                    bm_v3 dpos = v3_mul(v3_sub(v3((float)i, (float)j, (float)k), fx), M->dx);
+                    bm_v3 c = v3_mul(v3_add(momentum, m33_mul_v3(affine, dpos)), weight);
+                    int64_t at = ((int64_t)(base[0] + i) * M->dims[1] + (base[1] + j)) * M->dims[2] + (base[2] + k);
+                    int64_t cx = bm_fixed64(c.x, M->momentum_shift), cy = bm_fixed64(c.y, M->momentum_shift);
+                    int64_t cz = bm_fixed64(c.z, M->momentum_shift), cm = bm_fixed64(weight * M->mass, M->mass_shift);
+#pragma omp atomic
+                    T->grid_momentum[3 * at] += cx;
+#pragma omp atomic
+                    T->grid_momentum[3 * at + 1] += cy;
+#pragma omp atomic
+                    T->grid_momentum[3 * at + 2] += cz;
+#pragma omp atomic
+                    T->grid_mass[at] += cm;
+                }
+    }
+#pragma omp parallel for schedule(static)
+    for (node = 0; node < nodes; ++node) {
+        int kk = (int)(node % M->dims[2]), jj = (int)((node / M->dims[2]) % M->dims[1]);
+        int ii = (int)(node / ((int64_t)M->dims[1] * M->dims[2]));
+        float m = bm_unfixed64(T->grid_mass[node], M->mass_shift);
+        bm_v3 v = v3_zero();
+        if (m > 0.0f)
+            v = v3_div(v3(bm_unfixed64(T->grid_momentum[3 * node], M->momentum_shift),
+                          bm_unfixed64(T->grid_momentum[3 * node + 1], M->momentum_shift),
+                          bm_unfixed64(T->grid_momentum[3 * node + 2], M->momentum_shift)), m);
+        if (ii < 1 || jj < 1 || kk < 1 || ii >= M->dims[0] - 1 || jj >= M->dims[1] - 1 || kk >= M->dims[2] - 1) v = v3_zero();
+        st3(T->grid_v, node, v);
+    }
+#pragma omp parallel for schedule(static) reduction(+ : inversions)
+    for (p = 0; p < n; ++p) {
+        int base[3], i, j, k;
+        bm_v3 fx, new_v = v3_zero(), s, x = ld3(T->x, p);
+        bm_m33 new_C = m33_zero(), f, U, V;
+        float w[3][3], smallest, reference_J;
+        if (!mls_locate(M, x, base, &fx)) continue;
+        mls_weights(fx, w);
+        for (i = 0; i < 3; ++i)
+            for (j = 0; j < 3; ++j)
+                for (k = 0; k < 3; ++k) {
+                    float weight = (w[i][0] * w[j][1]) * w[k][2];
+                    bm_v3 dpos = v3_mul(v3_sub(v3((float)i, (float)j, (float)k), fx), M->dx);
+                    int64_t at = ((int64_t)(base[0] + i) * M->dims[1] + (base[1] + j)) * M->dims[2] + (base[2] + k);
+                    bm_v3 gv = ld3(T->grid_v, at);
+                    new_v = v3_add(new_v, v3_mul(gv, weight));
+                    new_C = m33_add(new_C, m33_scale(m33_outer(gv, dpos), (4.0f * weight) / (M->dx * M->dx)));
+                }
+        st3(T->v, p, new_v);
+        st9(T->C, p, new_C);
+        st3(T->x, p, v3_add(x, v3_mul(new_v, M->dt)));
+        f = m33_mul(m33_add(m33_identity(), m33_scale(new_C, M->dt)), ld9(T->F, p));
+        bm_svd3(f, &U, &s, &V);
+        smallest = bm_minf(bm_minf(s.x, s.y), s.z);
+        if (smallest <= 0.0f) inversions += 1;
+        if (smallest < 0.05f) {
+            s = v3(bm_maxf(s.x, 0.05f), bm_maxf(s.y, 0.05f), bm_maxf(s.z, 0.05f));
+            f = m33_mul(m33_mul(U, m33_diag(s)), m33_transpose(V));
+        }
+        reference_J = T->damage_reference[p];
+        if (M->plastic) {
+            bm_v3 e = v3(bm_logf(s.x), bm_logf(s.y), bm_logf(s.z)), dev;
+            float mean = ((e.x + e.y) + e.z) / 3.0f, norm, yield = T->yield_stress[p], limit;
+            dev = v3_sub(e, v3(mean, mean, mean));
+            norm = v3_len(dev);
+            limit = yield / (2.0f * M->mu) * sqrtf(2.0f / 3.0f);
+            if (norm > limit) {
+                e = v3_sub(e, v3_mul(dev, 1.0f - limit / norm));
+                s = v3(bm_expf(e.x), bm_expf(e.y), bm_expf(e.z));
+                f = m33_mul(m33_mul(U, m33_diag(s)), m33_transpose(V));
+                if (M->softening > 0.0f && reference_J > 0.0f) {
+                    float softened = bm_maxf(0.0f, yield - M->softening * (norm - limit));
+                    T->yield_stress[p] = softened;
+                    if (softened <= 0.0f) T->damage[p] = 1.0f;
+                }
+            }
+        }
+        st9(T->F, p, f);
+        if (reference_J > 0.0f) {
+            float J = ((s.x * s.y) * s.z) / reference_J;
+            if (J <= M->compressed || J >= M->stretched) T->damage[p] = 1.0f;
+        }
+    }
+    T->inversions[0] += inversions;
+}
+
 ORC_API int orc_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

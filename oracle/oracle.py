@@ -405,3 +405,107 @@ class OracleSolver:
 
 def config_dict(cfg):
     return asdict(cfg)
+
+
+class MlsState(ctypes.Structure):
+    _fields_ = [(name, P) for name in ("x", "v", "C", "F", "yield_stress", "damage", "damage_reference", "grid_mass",
+                                        "grid_momentum", "grid_v", "inversions")]
+
+
+class MlsOracle:
+    """MlsSolver (mlsmpm.py:232-446) restated on the CPU, particles in reference order (AoS)."""
+
+    def __init__(self, cfg, params=None, damage_from_start=True):
+        from blademaster_gb300.mlsmpm import TopoCutParams, fixed_shift, grid_layout
+
+        params = params or TopoCutParams()
+        L = self.L = lib()
+        if L.orc_mls_state_size() != ctypes.sizeof(MlsState):
+            raise RuntimeError("oracle MLS state layout mismatch")
+        L.orc_mls_substep.argtypes = [ctypes.POINTER(_native.MlsParams), ctypes.POINTER(MlsState),
+                                      ctypes.POINTER(_native.Params), ctypes.POINTER(State)]
+        L.orc_mls_substep.restype = None
+        self.config = cfg
+        dx = cfg.grid_spacing
+        reference, _, _ = points(cfg.size, dx, cfg.shape, cfg.sampling_seed)
+        self.reference = reference
+        n = self.n = len(reference)
+        volume = (dx / 2) ** 3
+        mass = cfg.density * volume
+        radius = dx / 4
+        blade_offset = max(cfg.blade_contact_radius or radius, radius - cfg.blade_half_size[0])
+        ratio = 1.0 if cfg.contact_reference_dt == 0 else (cfg.dt / cfg.contact_reference_dt) ** 2
+        sn, gk = cfg.normal_scale * ratio, cfg.tangent_stiffness * ratio
+        mu = cfg.young_modulus / (2 * (1 + cfg.poisson_ratio))
+        lam = cfg.young_modulus * cfg.poisson_ratio / ((1 + cfg.poisson_ratio) * (1 - 2 * cfg.poisson_ratio))
+        self.mass, self.mu = mass, mu
+        origin, dims = grid_layout(reference, dx, params)
+        self.origin, self.dims = origin, dims
+        nodes = int(np.prod(dims))
+        A = self.arrays = {}
+        A["x"] = np.ascontiguousarray(reference, np.float32)
+        A["v"] = np.zeros((n, 3), np.float32)
+        A["C"] = np.zeros((n, 9), np.float32)
+        A["F"] = np.tile(np.eye(3, dtype=np.float32).reshape(9), (n, 1))
+        A["yield_stress"] = np.full(n, cfg.yield_stress, np.float32)
+        A["damage"] = np.zeros(n, np.float32)
+        A["damage_reference"] = np.full(n, 1.0 if damage_from_start else 0.0, np.float32)
+        A["grid_mass"] = np.zeros(nodes, np.int64)
+        A["grid_momentum"] = np.zeros((nodes, 3), np.int64)
+        A["grid_v"] = np.zeros((nodes, 3), np.float32)
+        A["inversions"] = np.zeros(1, np.int32)
+        M = self.mls_params = _native.MlsParams()
+        M.n = n
+        for i in range(3):
+            M.dims[i], M.origin[i] = int(dims[i]), float(origin[i])
+        M.plastic = int(cfg.yield_stress > 0)
+        M.mass_shift = fixed_shift(float(np.float32(mass)))
+        M.momentum_shift = fixed_shift(float(np.float32(mass)) * dx / cfg.dt)
+        M.dx, M.dt, M.mass, M.volume, M.mu, M.lam = dx, cfg.dt, mass, volume, mu, lam
+        M.damaged_shear, M.softening = params.damaged_shear, params.softening
+        M.compressed = (1 - params.compression) ** params.sensitivity
+        M.stretched = (1 + params.stretch) ** params.sensitivity
+        T = self.mls_state = MlsState()
+        for name, _ in MlsState._fields_:
+            setattr(T, name, A[name].ctypes.data)
+        # contact state: one held knife (tool model -1, zero mobility), cutting off
+        p = self.contact_params = _native.Params()
+        p.n, p.tool_count, p.tool_model, p.external_tool = n, 1, -1, 1
+        p.dt, p.spacing, p.mass, p.volume, p.radius = cfg.dt, dx, mass, volume, radius
+        p.normal_scale, p.tangent_stiffness = sn, gk
+        p.friction_static, p.friction_dynamic, p.tangent_damping = cfg.friction_static, cfg.friction_dynamic, cfg.tangent_damping
+        p.board_scale = cfg.board_normal_scale or sn
+        p.board_half[0], p.board_half[1] = cfg.board_half_extent
+        for i in range(3):
+            p.half[i] = cfg.blade_half_size[i]
+        p.bevel, p.blade_offset, p.blade_mass, p.threshold = cfg.blade_bevel_height, blade_offset, cfg.blade_mass, 1.0
+        p.dt_d = float(np.float32(cfg.dt))
+        CA = self.contact = {name: np.zeros(4, np.int64) for name in _STATE_FIELDS}
+        CA["x"], CA["v"] = A["x"], A["v"]
+        CA["histories"] = np.zeros((2, n, 3), np.float32)
+        CA["damage"] = np.zeros((1, n), np.float32)
+        CA["impulses"] = np.zeros((n, 3), np.float32)
+        CA["tool"] = np.array([[0.0] * 9 + [1.0] + [0.0] * 3])
+        CA["mobility"] = np.zeros(36, np.float32)
+        CA["acc"] = np.zeros(_native.ACC_WORDS, np.uint64)
+        CA["interval"] = np.zeros(6)
+        CA["speed"] = np.zeros(1, np.float32)
+        CA["errors"] = np.zeros(3, np.int32)
+        CA["flags"] = np.zeros(_native.FLAG["WORDS"], np.int32)
+        S = self.contact_state = State()
+        for name in _STATE_FIELDS:
+            setattr(S, name, CA[name].ctypes.data)
+        S.capacity, S.buckets = 1, 1
+        self.step_count = 0
+
+    def advance(self, position, orientation_xyzw, velocity, angular, steps):
+        """`steps` substeps with the knife held at this state; returns (impulse, angular impulse)."""
+        packed = np.zeros(49, np.float32)
+        packed[:3], packed[3:7], packed[7:10], packed[10:13] = position, orientation_xyzw, velocity, angular
+        self.L.orc_load_external(ctypes.byref(self.contact_params), ctypes.byref(self.contact_state), ptr(packed))
+        for _ in range(steps):
+            self.L.orc_mls_substep(ctypes.byref(self.mls_params), ctypes.byref(self.mls_state),
+                                   ctypes.byref(self.contact_params), ctypes.byref(self.contact_state))
+        self.step_count += steps
+        interval = self.contact["interval"]
+        return interval[:3].copy(), interval[3:].copy()
