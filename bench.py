@@ -171,6 +171,76 @@ def cpu_baseline(name, seconds=15.0, max_steps=None):
     }
 
 
+def run_sweep(args, rank, world):
+    """Batched sweep of independent cutting instances (one graph launch per 1 ms interval) against the
+    same instances advanced one ExternalToolPort call at a time, as the reference's sweeps run."""
+    import torch
+
+    from blademaster_gb300.batch import BatchTuner, SolverBatch
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.solver import Solver
+    from blademaster_gb300.sweep import instances
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sweep = instances(args.instances, seed=rank)
+    solvers = [Solver(i.config, device=f"cuda:{local}") for i in sweep]
+    batch = SolverBatch(solvers)
+    steps = [int(round(0.001 / s.config.dt)) for s in solvers]
+    work = sum(s.n * k for s, k in zip(solvers, steps))
+    k = 0
+
+    def states():
+        nonlocal k
+        out = [i.state(k, start_gap=-0.001) for i in sweep]
+        k += 1
+        return out
+
+    tuner = BatchTuner(cache=os.path.join(tempfile.gettempdir(), "bm_tune.json"))
+    for lanes in tuner.candidates:  # first replays upload the graphs: keep them out of the tuning
+        if lanes <= len(solvers):
+            batch.advance(states(), 0.001, lanes=lanes, strict=False)
+    tuner.tune(batch, lambda i: states(), 0.001, strict=False)
+    for _ in range(args.warmup):
+        batch.advance(states(), 0.001, strict=False)
+    torch.cuda.synchronize()
+    begin = time.perf_counter()
+    for _ in range(args.steps):
+        batch.advance(states(), 0.001, strict=False)
+    batched = (time.perf_counter() - begin) / args.steps
+    ports = [ExternalToolPort(s) for s in solvers]
+
+    def port_interval(port, state):
+        try:
+            port.advance(state, 0.001)
+        except RuntimeError:  # the same checks as the batch's strict=False: the interval still ran
+            pass
+
+    for p, i in zip(ports, sweep):  # warm the per-instance graphs
+        port_interval(p, i.state(k, start_gap=-0.001))
+    k += 1
+    torch.cuda.synchronize()
+    begin = time.perf_counter()
+    for _ in range(max(1, args.steps // 4)):
+        for p, s_ in zip(ports, states()):
+            port_interval(p, s_)
+    single = (time.perf_counter() - begin) / max(1, args.steps // 4)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": world * work / batched, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": batched * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"sweep_{args.instances}_hcylinders", "instances": args.instances,
+                       "particles": sum(s.n for s in solvers), "substeps_per_interval": steps[0],
+                       "lanes": batch.lanes, "tuned": getattr(tuner, "timings", {}),
+                       "step": "one 1 ms coupling interval of every instance, host knife states in, reactions out"},
+            "per_instance": {"value": world * work / single, "ms_per_step": single * 1e3,
+                             "mode": "one ExternalToolPort.advance (graph) per instance per interval"},
+            "batched_speedup": single / batched,
+            "failed_instance_intervals": len(batch.failures),
+        }), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -210,6 +280,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="launch substeps without CUDA graphs (profiling)")
+    ap.add_argument("--instances", type=int, default=256, help="instances of the sweep_c4 workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -218,6 +289,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "sweep_c4":
+        run_sweep(args, rank, world)
         return
 
     import torch

@@ -182,6 +182,7 @@ def _declare(lib):
         "bm_graph_create": ([vp, ctypes.POINTER(StepArgs), vp, ctypes.POINTER(vp)], i),
         "bm_substeps_profiled": ([vp, ctypes.POINTER(StepArgs), vp, vp], i),
         "bm_graph_launch": ([vp, vp], i),
+        "bm_batch_graph_create": ([ctypes.POINTER(vp), ctypes.POINTER(StepArgs), i, i, vp, ctypes.POINTER(vp)], i),
         "bm_graph_destroy": ([vp], i),
         "bm_graph_kernel_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "bm_count_embedded": ([vp, i, vp], i),

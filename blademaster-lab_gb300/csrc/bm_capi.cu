@@ -334,6 +334,71 @@ int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_gra
     return BM_OK;
 }
 
+int bm_batch_graph_create(bm_solver* const* solvers, const bm_step_args* args, int count, int lanes, void* stream,
+                          bm_graph** out) {
+    if (!solvers || !args || !out || count < 1 || lanes < 1) return fail(BM_ERR_ARGUMENT, "invalid arguments");
+    for (int i = 0; i < count; ++i)
+        if (!solvers[i] || args[i].steps < 0) return fail(BM_ERR_ARGUMENT, "null solver or negative steps");
+    (void)stream;
+    if (lanes > count) lanes = count;
+    std::vector<cudaStream_t> lane(lanes, nullptr);
+    std::vector<cudaEvent_t> done(lanes, nullptr);
+    cudaStream_t origin = nullptr;
+    cudaEvent_t start = nullptr;
+    auto release = [&]() {
+        for (int l = 0; l < lanes; ++l) {
+            if (lane[l]) cudaStreamDestroy(lane[l]);
+            if (done[l]) cudaEventDestroy(done[l]);
+        }
+        if (origin) cudaStreamDestroy(origin);
+        if (start) cudaEventDestroy(start);
+    };
+    bool ok = cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&start, cudaEventDisableTiming) == cudaSuccess;
+    for (int l = 0; ok && l < lanes; ++l)
+        ok = cudaStreamCreateWithFlags(&lane[l], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&done[l], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        release();
+        return check_cuda("batch streams");
+    }
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        release();
+        return check_cuda("begin capture");
+    }
+    cudaEventRecord(start, origin);
+    for (int l = 0; l < lanes; ++l) cudaStreamWaitEvent(lane[l], start, 0);
+    int rc = BM_OK;
+    for (int i = 0; i < count && rc == BM_OK; ++i) rc = run_batch(solvers[i], &args[i], lane[i % lanes]);
+    for (int l = 0; l < lanes; ++l) {
+        cudaEventRecord(done[l], lane[l]);
+        cudaStreamWaitEvent(origin, done[l], 0);
+    }
+    const cudaError_t e = cudaStreamEndCapture(origin, &graph);
+    release();
+    if (rc != BM_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return check_cuda("end capture");
+    cudaGraphExec_t exec;
+    if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return check_cuda("graph instantiate");
+    }
+    bm_graph* g = new (std::nothrow) bm_graph;
+    if (!g) {
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        return fail(BM_ERR_STATE, "out of host memory");
+    }
+    g->graph = graph;
+    g->exec = exec;
+    *out = g;
+    return BM_OK;
+}
+
 int bm_graph_launch(bm_graph* g, void* stream) {
     if (!g) return fail(BM_ERR_ARGUMENT, "null graph");
     cudaGraphLaunch(g->exec, as_stream(stream));

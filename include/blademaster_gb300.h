@@ -286,6 +286,15 @@ int bm_substeps(bm_solver* s, const bm_step_args* args, void* stream);
 int bm_graph_create(bm_solver* s, const bm_step_args* args, void* stream, bm_graph** out);
 int bm_graph_launch(bm_graph* g, void* stream);
 int bm_graph_destroy(bm_graph* g);
+/* Batched sweeps: the batches of `count` independent solvers captured as one
+ * CUDA graph, so one bm_graph_launch advances every instance (no reference
+ * counterpart: the reference runs sweep instances one after another,
+ * scripts/force_convergence.py:92-129).  Each solver's chain of kernels is an
+ * independent branch; the chains are captured on `lanes` streams in the
+ * given order (solver i on lane i % lanes), which sets how many run
+ * concurrently.  args[i] are solver i's batch arguments. */
+int bm_batch_graph_create(bm_solver* const* solvers, const bm_step_args* args, int count, int lanes, void* stream,
+                          bm_graph** out);
 /* Number of kernel launches one bm_graph_launch of `g` performs (its kernel nodes). */
 int bm_graph_kernel_count(const bm_graph* g, int64_t* count);
 /* Stages of one substep, in launch order (profiling). */
