@@ -809,7 +809,8 @@ __device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const
     if (relax > 0.0f) {
         const bm_v3 step = v3_mul(dev, relax);
         dev = v3_sub(dev, step);
-        const bm_v3 growth = v3(bm_expm1f(-step.x), bm_expm1f(-step.y), bm_expm1f(-step.z));
+        // f_m <- f_m W with W = Vm diag(exp(-step)) Vm^T, i.e. Fv <- W^-1 Fv (material.py:518-521)
+        const bm_v3 growth = v3(bm_expm1f(step.x), bm_expm1f(step.y), bm_expm1f(step.z));
         const bm_m33 delta = m33_mul(m33_mul(Vm, m33_diag(growth)), m33_transpose(Vm));
         double dd[9], nd[9];
         for (int r = 0; r < 3; ++r)

@@ -305,7 +305,8 @@ static void maxwell_at(const bm_params* P, orc_state* S, int64_t p, bm_m33 U, bm
         bm_m33 delta;
         double dd[9], nd[9];
         dev = v3_sub(dev, step);
-        growth = v3(bm_expm1f(-step.x), bm_expm1f(-step.y), bm_expm1f(-step.z));
+        /* f_m <- f_m W with W = Vm diag(exp(-step)) Vm^T, i.e. Fv <- W^-1 Fv (material.py:518-521) */
+        growth = v3(bm_expm1f(step.x), bm_expm1f(step.y), bm_expm1f(step.z));
         delta = m33_mul(m33_mul(Vm, m33_diag(growth)), m33_transpose(Vm));
         for (r = 0; r < 3; ++r) for (c = 0; c < 3; ++c) dd[3 * r + c] = (double)delta.m[r][c];
         /* D + delta + delta D in float64 */
@@ -355,6 +356,16 @@ ORC_API void orc_refresh_stress(const bm_params* P, orc_state* S) {
         if (P->maxwell) maxwell_stress_at(P, S, p, 0.0f, &S->errors[1]);
         else stress_at(P, S, p, &S->errors[1]);
     }
+}
+
+/* update_F_maxwell (material.py:592-618) with a zero velocity gradient, `steps`
+ * times: F is held and only the Maxwell branch relaxes (the reference's
+ * hold_step, tests/test_maxwell.py:49-69). */
+ORC_API void orc_maxwell_hold(const bm_params* P, orc_state* S, int steps) {
+    int64_t p;
+    int k;
+    for (k = 0; k < steps; ++k)
+        for (p = 0; p < P->n; ++p) maxwell_stress_at(P, S, p, P->maxwell_relax, &S->errors[1]);
 }
 
 /* material.plastic_project (material.py:434-442). */

@@ -106,6 +106,8 @@ def lib():
         L.orc_fx_roundtrip.argtypes = [vp, i, vp]
         for name in ("orc_couple_fields", "orc_g2p", "orc_math_f", "orc_math_d", "orc_svd", "orc_fx_roundtrip"):
             getattr(L, name).restype = None
+        L.orc_maxwell_hold.argtypes = [pp, ps, i]
+        L.orc_maxwell_hold.restype = None
         L.orc_count_embedded.argtypes = [pp, ps]
         L.orc_count_embedded.restype = ctypes.c_int64
         L.orc_num_threads.restype = ctypes.c_int
