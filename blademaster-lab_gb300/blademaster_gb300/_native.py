@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_capi.cu", "bm_noalloc.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -168,6 +168,7 @@ def _declare(lib):
         "bm_particle_contacts": ([vp, vp], i),
         "bm_particle_contacts_static": ([vp, vp], i),
         "bm_hold_constraint": ([vp, vp], i),
+        "bm_gemm_tn_bf16": ([vp, vp, vp, i, i, i, vp, i, vp, vp, vp], i),
         "bm_mls_create": ([ctypes.POINTER(MlsParams), ctypes.POINTER(MlsBuffers), ctypes.POINTER(Params),
                            ctypes.POINTER(Buffers), ctypes.POINTER(vp)], i),
         "bm_mls_destroy": ([vp], i),

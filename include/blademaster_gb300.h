@@ -403,6 +403,18 @@ int bm_mls_substeps(bm_mls* s, int steps, void* stream);
 /* The same interval captured as a CUDA graph (MlsSolver.advance, mlsmpm.py:395-426). */
 int bm_mls_graph_create(bm_mls* s, int steps, void* stream, bm_graph** out);
 
+/* ------------------------------------------------------------------------
+ * Learned tool predictor (no reference counterpart: it stands in for the
+ * linear mobility prediction of tool_substep "predict", tool.py:97-113).
+ * ------------------------------------------------------------------------ */
+/* D[M x N] = A[M x K] * B[N x K]^T on the tensor cores (tcgen05): A and B
+ * bf16, row-major (K contiguous), fp32 accumulation, then + bias[N] and ReLU
+ * if requested; D (fp32) and/or D_bf16 receive the result.  N in 16..256 (a
+ * multiple of 16), K a multiple of 32, all rows 16-byte aligned.  *status is
+ * set to 1 if the tensor-core work did not complete in time. */
+int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, const float* bias, int relu,
+                    uint16_t* D_bf16, int32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
