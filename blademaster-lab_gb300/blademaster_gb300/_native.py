@@ -169,6 +169,13 @@ def _declare(lib):
         "bm_particle_contacts_static": ([vp, vp], i),
         "bm_hold_constraint": ([vp, vp], i),
         "bm_gemm_tn_bf16": ([vp, vp, vp, i, i, i, vp, i, vp, vp, vp], i),
+        "bm_mlp_transpose16": ([vp, vp, i, i, vp], i),
+        "bm_mlp_relu_grad": ([vp, vp, vp, ctypes.c_int64, vp], i),
+        "bm_mlp_pool": ([vp, i, vp, f, f, vp, vp], i),
+        "bm_mlp_mse_grad": ([vp, vp, i, i, i, vp, vp, vp, vp], i),
+        "bm_mlp_colsum": ([vp, i, i, vp, vp], i),
+        "bm_mlp_cast_bf16": ([vp, i, i, i, vp, vp], i),
+        "bm_mlp_adam": ([vp, vp, vp, vp, vp, ctypes.c_int64, f, f, f, f, i, vp], i),
         "bm_mls_create": ([ctypes.POINTER(MlsParams), ctypes.POINTER(MlsBuffers), ctypes.POINTER(Params),
                            ctypes.POINTER(Buffers), ctypes.POINTER(vp)], i),
         "bm_mls_destroy": ([vp], i),

@@ -172,10 +172,174 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
+// ---------------------------------------------------------------- training
+
+__device__ __forceinline__ uint16_t to_bf16(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
+__device__ __forceinline__ float from_bf16(uint16_t v) { return __bfloat162float(__ushort_as_bfloat16(v)); }
+
+// out[c][r] = in[r][c] (bf16 bits), 32 x 32 tiles through shared memory.
+__global__ void k_transpose16(const uint16_t* __restrict__ in, uint16_t* __restrict__ out, int rows, int cols) {
+    __shared__ uint16_t tile[32][33];
+    const int c = blockIdx.x * 32 + threadIdx.x, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+        if (r0 + i < rows && c < cols) tile[i][threadIdx.x] = in[(int64_t)(r0 + i) * cols + c];
+    __syncthreads();
+    const int r = r0 + threadIdx.x, c0 = blockIdx.x * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+        if (c0 + i < cols && r < rows) out[(int64_t)(c0 + i) * rows + r] = tile[threadIdx.x][i];
+}
+
+// Gradient through a ReLU layer: g[i] *= (h[i] > 0) in place (h is the layer's bf16
+// output), and the result as bf16 in out.
+__global__ void k_relu_grad(float* __restrict__ g, const uint16_t* __restrict__ h, uint16_t* __restrict__ out,
+                            int64_t count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = from_bf16(h[i]) > 0.0f ? g[i] : 0.0f;
+        g[i] = v;
+        out[i] = to_bf16(v);
+    }
+}
+
+// Occupancy of 4 x 4 x 4 bins in the knife's frame around its edge: local =
+// rot^-1 (x - edge); bin i spans [-4 h, 4 h) across the blade (x), the
+// blade length [-half_y, half_y) (y) and [-4 h, 4 h) about the edge (z).
+// Particle counts (exact integer sums) per bin.
+__global__ void k_pool(const float* __restrict__ x, int n, const float* __restrict__ tool_f, float h, float half_y,
+                       int32_t* __restrict__ counts) {
+    const ToolF T = load_tool(tool_f);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const bm_v3 local = q_rotate_inv(T.rot, v3_sub(ld3(x, n, p), T.edge));
+        const float fx = (local.x + 4.0f * h) / (2.0f * h), fy = (local.y + half_y) / (0.5f * half_y),
+                    fz = (local.z + 4.0f * h) / (2.0f * h);
+        if (!(fx >= 0.0f && fx < 4.0f && fy >= 0.0f && fy < 4.0f && fz >= 0.0f && fz < 4.0f)) continue;
+        atomicAdd(&counts[((int)fx * 4 + (int)fy) * 4 + (int)fz], 1);
+    }
+}
+
+// Loss gradient of the mean squared error over rows x outputs (outputs of `width` columns,
+// `pad` columns stored): d = 2 (y - t) / (rows * outputs), as fp32 and bf16; padded columns 0.
+// Also sums the loss (fp32 per row, then one atomic per block).
+__global__ void k_mse_grad(const float* __restrict__ y, const float* __restrict__ t, int rows, int outputs, int width,
+                           float* __restrict__ d, uint16_t* __restrict__ dh, float* loss) {
+    __shared__ float part[256];
+    float local = 0.0f;
+    const float scale = 2.0f / ((float)rows * (float)outputs);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)rows * width;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / width), c = (int)(i % width);
+        float g = 0.0f;
+        if (c < outputs) {
+            const float e = y[i] - t[(int64_t)r * outputs + c];
+            local += e * e;
+            g = scale * e;
+        }
+        d[i] = g;
+        dh[i] = to_bf16(g);
+    }
+    part[threadIdx.x] = local;
+    __syncthreads();
+    for (int step = blockDim.x / 2; step > 0; step >>= 1) {
+        if (threadIdx.x < step) part[threadIdx.x] += part[threadIdx.x + step];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && loss) atomicAdd(loss, part[0] / ((float)rows * (float)outputs));
+}
+
+// Column sums of a [rows x cols] fp32 matrix (bias gradients), one thread per column, rows in order.
+__global__ void k_colsum(const float* __restrict__ g, int rows, int cols, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.0f;
+    for (int r = 0; r < rows; ++r) s += g[(int64_t)r * cols + c];
+    out[c] = s;
+}
+
+// bf16 bits of x (fp32) with a row stride conversion: out[r][c] for c < cols, 0 for cols <= c < pitch.
+__global__ void k_cast_bf16(const float* __restrict__ x, int rows, int cols, int pitch, uint16_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)rows * pitch;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / pitch), c = (int)(i % pitch);
+        out[i] = c < cols ? to_bf16(x[(int64_t)r * cols + c]) : (uint16_t)0;
+    }
+}
+
+// Adam (Kingma and Ba 2015) on fp32 master weights; writes the bf16 copy used by the GEMMs.
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       uint16_t* __restrict__ wh, int64_t count, float lr, float beta1, float beta2, float eps,
+                       float correction1, float correction2) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = beta1 * m[i] + (1.0f - beta1) * gi;
+        const float vi = beta2 * v[i] + (1.0f - beta2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / correction1) / (sqrtf(vi / correction2) + eps);
+        w[i] = wi;
+        if (wh) wh[i] = to_bf16(wi);
+    }
+}
+
 }  // namespace
 }  // namespace bm
 
 extern "C" {
+
+int bm_mlp_transpose16(const uint16_t* in, uint16_t* out, int rows, int cols, void* stream) {
+    if (!in || !out || rows < 0 || cols < 0) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    if (!rows || !cols) return BM_OK;
+    const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32)), block(32, 8);
+    bm::k_transpose16<<<grid, block, 0, reinterpret_cast<cudaStream_t>(stream)>>>(in, out, rows, cols);
+    return bm::check_cuda("mlp_transpose16");
+}
+
+int bm_mlp_relu_grad(float* g, const uint16_t* h, uint16_t* out, int64_t count, void* stream) {
+    if (!g || !h || !out || count < 0) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    if (!count) return BM_OK;
+    bm::k_relu_grad<<<bm::grid_for(count) < 1216 ? bm::grid_for(count) : 1216, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(g, h, out, count);
+    return bm::check_cuda("mlp_relu_grad");
+}
+
+int bm_mlp_pool(const float* x, int n, const float* tool_f, float h, float half_y, int32_t* counts, void* stream) {
+    if (!x || !tool_f || !counts || n < 0 || !(h > 0.0f) || !(half_y > 0.0f)) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaMemsetAsync(counts, 0, 64 * sizeof(int32_t), st);
+    if (n) bm::k_pool<<<bm::grid_for(n) < 608 ? bm::grid_for(n) : 608, 256, 0, st>>>(x, n, tool_f, h, half_y, counts);
+    return bm::check_cuda("mlp_pool");
+}
+
+int bm_mlp_mse_grad(const float* y, const float* t, int rows, int outputs, int width, float* d, uint16_t* d_bf16,
+                    float* loss, void* stream) {
+    if (!y || !t || !d || !d_bf16 || rows < 1 || outputs < 1 || width < outputs) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    const int64_t count = (int64_t)rows * width;
+    bm::k_mse_grad<<<bm::grid_for(count) < 608 ? bm::grid_for(count) : 608, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        y, t, rows, outputs, width, d, d_bf16, loss);
+    return bm::check_cuda("mlp_mse_grad");
+}
+
+int bm_mlp_colsum(const float* g, int rows, int cols, float* out, void* stream) {
+    if (!g || !out || rows < 0 || cols < 1) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    bm::k_colsum<<<(cols + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(g, rows, cols, out);
+    return bm::check_cuda("mlp_colsum");
+}
+
+int bm_mlp_cast_bf16(const float* x, int rows, int cols, int pitch, uint16_t* out, void* stream) {
+    if (!x || !out || rows < 0 || cols < 0 || pitch < cols) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    const int64_t count = (int64_t)rows * pitch;
+    if (!count) return BM_OK;
+    bm::k_cast_bf16<<<bm::grid_for(count) < 1216 ? bm::grid_for(count) : 1216, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        x, rows, cols, pitch, out);
+    return bm::check_cuda("mlp_cast_bf16");
+}
+
+int bm_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* w_bf16, int64_t count, float lr, float beta1,
+                float beta2, float eps, int step, void* stream) {
+    if (!w || !g || !m || !v || count < 0 || step < 1) return bm::fail(BM_ERR_ARGUMENT, "invalid arguments");
+    if (!count) return BM_OK;
+    const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    bm::k_adam<<<bm::grid_for(count) < 1216 ? bm::grid_for(count) : 1216, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        w, g, m, v, w_bf16, count, lr, beta1, beta2, eps, c1, c2);
+    return bm::check_cuda("mlp_adam");
+}
 
 int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, const float* bias, int relu,
                     uint16_t* D_bf16, int32_t* status, void* stream) {

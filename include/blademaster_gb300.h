@@ -414,6 +414,23 @@ int bm_mls_graph_create(bm_mls* s, int steps, void* stream, bm_graph** out);
  * set to 1 if the tensor-core work did not complete in time. */
 int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, const float* bias, int relu,
                     uint16_t* D_bf16, int32_t* status, void* stream);
+/* Training kernels of the predictor: bf16 transpose ([rows x cols] -> [cols x rows]),
+ * ReLU backward (g * (h > 0) to bf16), mean-squared-error gradient over `outputs`
+ * of `width` stored columns (adds the loss to *loss), column sums, fp32 -> bf16
+ * with a padded row pitch, and one Adam step (bias-corrected, step >= 1). */
+int bm_mlp_transpose16(const uint16_t* in, uint16_t* out, int rows, int cols, void* stream);
+int bm_mlp_relu_grad(float* g, const uint16_t* h, uint16_t* out, int64_t count, void* stream);
+/* Predictor input: particle counts of 4 x 4 x 4 bins in the frame of knife 0
+ * (tool_f, one BM_TOOL_F_WORDS record) around its edge, x in [-4h, 4h) across
+ * the blade, y in [-half_y, half_y), z in [-4h, 4h) about the edge;
+ * x is [3][n]; counts[64] are overwritten. */
+int bm_mlp_pool(const float* x, int n, const float* tool_f, float h, float half_y, int32_t* counts, void* stream);
+int bm_mlp_mse_grad(const float* y, const float* t, int rows, int outputs, int width, float* d, uint16_t* d_bf16,
+                    float* loss, void* stream);
+int bm_mlp_colsum(const float* g, int rows, int cols, float* out, void* stream);
+int bm_mlp_cast_bf16(const float* x, int rows, int cols, int pitch, uint16_t* out, void* stream);
+int bm_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* w_bf16, int64_t count, float lr, float beta1,
+                float beta2, float eps, int step, void* stream);
 
 #ifdef __cplusplus
 }
