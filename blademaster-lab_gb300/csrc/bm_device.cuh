@@ -63,47 +63,58 @@ struct ToolF {
     bm_v3 edge_vel;     // vel + omega x (edge - pos)
     bm_v3 ax, ay, az;   // knife axes in the world (for conservative pre-tests only)
 };
+// The record is read as nine 16-byte loads (records are 144 bytes, 16-byte aligned).
 __device__ __forceinline__ ToolF load_tool(const float* __restrict__ t) {
+    const float4* q = reinterpret_cast<const float4*>(t);
+    const float4 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4], f = q[5], g = q[6], h = q[7], i = q[8];
     ToolF r;
-    r.pos = v3(t[0], t[1], t[2]);
-    r.vel = v3(t[3], t[4], t[5]);
-    r.rot.x = t[6];
-    r.rot.y = t[7];
-    r.rot.z = t[8];
-    r.rot.w = t[9];
-    r.omega = v3(t[10], t[11], t[12]);
-    r.speed = t[13];
-    r.spin_reach = t[14];
-    r.edge = v3(t[15], t[16], t[17]);
-    r.down = v3(t[18], t[19], t[20]);
-    r.edge_vel = v3(t[21], t[22], t[23]);
-    r.ax = v3(t[24], t[25], t[26]);
-    r.ay = v3(t[27], t[28], t[29]);
-    r.az = v3(t[30], t[31], t[32]);
+    r.pos = v3(a.x, a.y, a.z);
+    r.vel = v3(a.w, b.x, b.y);
+    r.rot.x = b.z;
+    r.rot.y = b.w;
+    r.rot.z = c.x;
+    r.rot.w = c.y;
+    r.omega = v3(c.z, c.w, d.x);
+    r.speed = d.y;
+    r.spin_reach = d.z;
+    r.edge = v3(d.w, e.x, e.y);
+    r.down = v3(e.z, e.w, f.x);
+    r.edge_vel = v3(f.y, f.z, f.w);
+    r.ax = v3(g.x, g.y, g.z);
+    r.ay = v3(g.w, h.x, h.y);
+    r.az = v3(h.z, h.w, i.x);
     return r;
 }
 __device__ __forceinline__ float blade_radius(const bm_params& P) {
     return sqrtf((P.half[0] * P.half[0] + P.half[1] * P.half[1]) + P.half[2] * P.half[2]);
 }
 
+// Signed-integer keys that order like the floats (and back).
+__device__ __forceinline__ int order_key(float f) {
+    const int b = __float_as_int(f);
+    return b ^ ((b >> 31) & 0x7FFFFFFF);
+}
+__device__ __forceinline__ float order_value(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7FFFFFFF)); }
+
 // Bounding box (centre, half extent) of the positions of this warp's active
 // lanes and the largest of their `speed` values.  All 32 lanes must call;
 // `*any` is false when no lane is active.  The box is widened by 1 um so that
 // it still contains every position after the rounding of centre and extent.
+// Minima and maxima are exact (integer warp reductions of order keys).
 __device__ __forceinline__ void warp_box(bm_v3 x, float speed, bool active, bm_v3* centre, bm_v3* extent,
                                          float* max_speed, bool* any) {
-    const float inf = 3.0e38f;
-    float v[7] = {active ? x.x : inf,  active ? x.y : inf,  active ? x.z : inf,   active ? -x.x : inf,
-                  active ? -x.y : inf, active ? -x.z : inf, active ? -speed : inf};
-#pragma unroll
-    for (int i = 0; i < 7; ++i)
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) v[i] = fminf(v[i], __shfl_xor_sync(0xffffffffu, v[i], d));
-    *any = v[0] < inf;
-    const bm_v3 lo = v3(v[0], v[1], v[2]), hi = v3(-v[3], -v[4], -v[5]);
+    const unsigned all = 0xffffffffu;
+    *any = __any_sync(all, active);
+    const int big = 0x7fffffff, small = (int)0x80000000;
+    const bm_v3 lo = v3(order_value(__reduce_min_sync(all, active ? order_key(x.x) : big)),
+                        order_value(__reduce_min_sync(all, active ? order_key(x.y) : big)),
+                        order_value(__reduce_min_sync(all, active ? order_key(x.z) : big)));
+    const bm_v3 hi = v3(order_value(__reduce_max_sync(all, active ? order_key(x.x) : small)),
+                        order_value(__reduce_max_sync(all, active ? order_key(x.y) : small)),
+                        order_value(__reduce_max_sync(all, active ? order_key(x.z) : small)));
     *centre = v3_mul(v3_add(lo, hi), 0.5f);
     *extent = v3_add(v3_mul(v3_sub(hi, lo), 0.5f), v3(1.0e-6f, 1.0e-6f, 1.0e-6f));
-    *max_speed = -v[6];
+    *max_speed = order_value(__reduce_max_sync(all, active ? order_key(speed) : small));
 }
 
 // Projection radius of a box with half extent e on direction a.

@@ -730,8 +730,8 @@ __global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) 
 // P = 2 mu (f - R) + lam (J - 1) J f^-T, equal to material.corotated_stress
 // (material.py:78-91) with Fp = I.
 __device__ __forceinline__ bm_m33 corotated_polar(const bm_m33& f, float J, float mu, float lam) {
-    const bm_m33 R = bm_polar3(f);
-    const bm_m33 inv_t = m33_transpose(m33_inverse(f));
+    bm_m33 inv_t;  // f^-T, the polar iteration's first inverse transpose
+    const bm_m33 R = bm_polar3_inv(f, &inv_t);
     const float c = lam * (J - 1.0f) * J, two_mu = 2.0f * mu;
     bm_m33 out;
 #pragma unroll

@@ -362,11 +362,18 @@ BM_HD bm_qd qd_from_axis_angle(bm_v3d axis, double angle) {
  * an update of size d leaves an error of about d^2 / 2, so the iteration
  * stops after an update below 1e-4 (remaining error < 1e-8, below float
  * resolution), or after 16 iterations. */
+BM_HD bm_m33 bm_polar3_inv(bm_m33 a, bm_m33* first_inv_t);
 BM_HD bm_m33 bm_polar3(bm_m33 a) {
+    bm_m33 unused;
+    return bm_polar3_inv(a, &unused);
+}
+/* bm_polar3, also returning a^-T (the first iteration's inverse transpose). */
+BM_HD bm_m33 bm_polar3_inv(bm_m33 a, bm_m33* first_inv_t) {
     bm_m33 x = a, y;
     int it, i, j;
     for (it = 0; it < 16; ++it) {
         bm_m33 inv_t = m33_transpose(m33_inverse(x));
+        if (it == 0) *first_inv_t = inv_t;
         float change = 0.0f;
         for (i = 0; i < 3; ++i)
             for (j = 0; j < 3; ++j) {
