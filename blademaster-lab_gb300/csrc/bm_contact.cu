@@ -290,7 +290,7 @@ __device__ unsigned rigid_knives(const bm_params& P, const bm_buffers& B, bm_v3 
 }
 
 // contact.rigid_and_speed + extra_blade (contact.py:422-566) for every knife.
-__global__ void k_rigid(bm_params P, bm_buffers B, int cutting) {
+__global__ void __launch_bounds__(256, 4) k_rigid(bm_params P, bm_buffers B, int cutting) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = p < P.n;
     const int64_t N = P.n;
