@@ -968,7 +968,7 @@ __device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
 // with this substep's side labelling (run after the tool update); thread 0
 // advances the substep counter of the friction-history ping-pong.
-__global__ void __launch_bounds__(256, 3) k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting, int advance_step) {
+__global__ void __launch_bounds__(256, 4) k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting, int advance_step) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
     const bool active = p < P.n;
