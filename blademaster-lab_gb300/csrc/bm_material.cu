@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int
 // fetches one corner value, then the lane of corner 0 of each field adds the
 // eight in ascending cell index (a = 7 .. 0); fields are taken four at a time.
 // Then lane f evaluates the exchange of field f (couple_and_velocity_at).
-__global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
+__global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B, int write_sums) {
     const int count = B.flags[BM_FLAG_MULTI];
     const int S = P.fmax * P.node_count;
     const int lane = threadIdx.x & 31;
@@ -503,6 +503,49 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
                     if (use) sum[v] = sum[v] + x;
                 }
             }
+            if (nf <= 4) {
+                // every field's sums are in this warp (lane group g holds field g): exchange by
+                // shuffles in ascending field order, as the general path below does from memory
+                const int slot = f * P.node_count + n;
+                const float ma = sum[0];
+                const bm_v3 pa = v3(sum[1], sum[2], sum[3]), ja = v3(sum[4], sum[5], sum[6]);
+                uint64_t oa = 0u, ta = 0u;
+                if (f < nf) {
+                    oa = B.fones[slot];
+                    ta = B.ftwos[slot];
+                }
+                float total = 0.0f;
+                bm_v3 dm = v3_zero(), di = v3_zero();
+                for (int g = 0; g < nf; ++g) {
+                    const int src = 8 * g;
+                    const float mb = __shfl_sync(kFull, ma, src);
+                    const bm_v3 pb = v3(__shfl_sync(kFull, pa.x, src), __shfl_sync(kFull, pa.y, src), __shfl_sync(kFull, pa.z, src));
+                    const bm_v3 jb = v3(__shfl_sync(kFull, ja.x, src), __shfl_sync(kFull, ja.y, src), __shfl_sync(kFull, ja.z, src));
+                    const uint64_t ob = __shfl_sync(kFull, oa, src), tb = __shfl_sync(kFull, ta, src);
+                    total = total + mb;
+                    if (g != f && compatible_masks(oa, ta, ob, tb)) {
+                        dm = v3_add(dm, v3_sub(v3_mul(pb, ma), v3_mul(pa, mb)));
+                        di = v3_add(di, v3_sub(v3_mul(jb, ma), v3_mul(ja, mb)));
+                    }
+                }
+                if (a == 0 && f < nf) {
+                    B.grid_mass[slot] = ma;
+                    if (write_sums) {
+                        st3(B.momentum, S, slot, pa);
+                        st3(B.grid_impulse, S, slot, ja);
+                    }
+                    if (ma <= 0.0f) {
+                        st3(B.old_v, S, slot, v3_zero());
+                        st3(B.new_v, S, slot, v3_zero());
+                    } else {
+                        const bm_v3 pm = v3_add(pa, v3_div(dm, total));
+                        const bm_v3 jm = v3_add(ja, v3_div(di, total));
+                        st3(B.old_v, S, slot, v3_div(pm, ma));
+                        st3(B.new_v, S, slot, v3_div(v3_add(pm, jm), ma));
+                    }
+                }
+                continue;
+            }
             if (a == 0 && f < nf) {
                 const int slot = f * P.node_count + n;
                 B.grid_mass[slot] = sum[0];
@@ -510,6 +553,7 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B) {
                 st3(B.grid_impulse, S, slot, v3(sum[4], sum[5], sum[6]));
             }
         }
+        if (nf <= 4) continue;
         __syncwarp();
         // exchange (couple_and_velocity_at): lane f handles field f
         for (int f = lane; f < nf; f += 32) {
@@ -697,8 +741,37 @@ __global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) 
                     if (use) sum[v] = sum[v] + x;
                 }
             }
+            if (nf <= 4) {
+                // couple (couple_at) by shuffles, ascending field order as in the general path
+                const int sa = f * P.node_count + n;
+                float ma = 0.0f;
+                uint64_t oa = 0u, ta = 0u;
+                if (f < nf) {
+                    ma = B.grid_mass[sa];
+                    oa = B.fones[sa];
+                    ta = B.ftwos[sa];
+                }
+                const bm_v3 va = v3(sum[0], sum[1], sum[2]);
+                float total = 0.0f;
+                bm_v3 ex = v3_zero();
+                for (int g = 0; g < nf; ++g) {
+                    const int src = 8 * g;
+                    const float mb = __shfl_sync(kFull, ma, src);
+                    const bm_v3 vb = v3(__shfl_sync(kFull, va.x, src), __shfl_sync(kFull, va.y, src), __shfl_sync(kFull, va.z, src));
+                    const uint64_t ob = __shfl_sync(kFull, oa, src), tb = __shfl_sync(kFull, ta, src);
+                    total = total + mb;
+                    if (g != f && compatible_masks(oa, ta, ob, tb)) ex = v3_add(ex, v3_sub(v3_mul(vb, ma), v3_mul(va, mb)));
+                }
+                if (a == 0 && f < nf) {
+                    st3(B.remapped, S, sa, va);
+                    if (ma <= 0.0f) st3(B.remap_v, S, sa, v3_zero());
+                    else st3(B.remap_v, S, sa, v3_div(v3_add(va, v3_div(ex, total)), ma));
+                }
+                continue;
+            }
             if (a == 0 && f < nf) st3(B.remapped, S, f * P.node_count + n, v3(sum[0], sum[1], sum[2]));
         }
+        if (nf <= 4) continue;
         __syncwarp();
         for (int f = lane; f < nf; f += 32) {
             const int sa = f * P.node_count + n;
@@ -1115,7 +1188,7 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
     k_p2g_mixed_cells<<<2 * 152, kBlock, 0, st>>>(P, B);
     k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
-    k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B);
+    k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
     if (P.viscous) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
