@@ -358,9 +358,13 @@ def main():
         ms = float(t.item())
     slots = int(s._t["nfield"].sum().item())
     counters_after = s._t["flags"].cpu().numpy()
+    def delta(name):
+        return int(counters_after[_native.FLAG[name]] - counters_before[_native.FLAG[name]])
+
     events = {
-        "pair_list_builds": int(counters_after[_native.FLAG["PAIR_BUILDS"]] - counters_before[_native.FLAG["PAIR_BUILDS"]]),
-        "registrations": int(counters_after[_native.FLAG["REGISTRATIONS"]] - counters_before[_native.FLAG["REGISTRATIONS"]]),
+        "pair_list_builds": delta("PAIR_BUILDS"),
+        "relists": delta("RELISTS"),
+        "registrations": delta("REGISTRATIONS"),
         "multi_field_nodes": int(counters_after[_native.FLAG["MULTI"]]),
         "mixed_cells": int(counters_after[_native.FLAG["MIXED_CELLS"]]),
     }

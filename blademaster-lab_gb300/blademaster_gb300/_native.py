@@ -142,7 +142,7 @@ TOOL_F_WORDS = int(header_constant("BM_TOOL_F_WORDS"))
 FLAG = {
     k: int(header_constant("BM_FLAG_" + k))
     for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "CHANGED",
-              "RELIST", "MULTI", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "HOLD_NEEDS",
+              "RELIST", "MULTI", "RELISTS", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "HOLD_NEEDS",
               "HOLD_RESIDUAL", "HOLD_COUNT", "HOLD_NODES", "WORDS")
 }
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4

@@ -44,7 +44,7 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int64_t tiles_of(const bm_params& P) { return ((int64_t)P.bucket_mask + 1 + 1023) / 1024; }
 
 void layout_scratch(bm_solver* s) {
-    // [0] pair reach (float), [64 .. 64 + tiles) scan partials, then 9 n floats (viscous stress).
+    // [0] pair reach (float), [1] scan ticket, [64 .. 64 + tiles) scan partials, then 9 n floats (viscous stress).
     int32_t* base = s->B.scratch;
     s->scan_partials = base + 64;
     int64_t off = 64 + tiles_of(s->P);
@@ -61,18 +61,33 @@ struct StageTimer {
     }
 };
 
+int64_t kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return -1;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return -1;
+    int64_t kernels = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType type;
+        if (cudaGraphNodeGetType(nodes[i], &type) != cudaSuccess) return -1;
+        if (type == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    return kernels;
+}
+
 // One batch of substeps on stream st.
 int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* timer = nullptr,
               float* stage_ms = nullptr) {
     const bm_params& P = s->P;
     const int64_t* field_codes = a->single_field ? s->B.zero_codes : s->B.codes;
+    const bool force_topology = !P.cache_topology;
     StageTimer none;
     StageTimer& t = timer ? *timer : none;
     if (a->external_load) bm::launch_load_external(s, st);
     if (a->record_samples) bm::launch_record_pose(s, 0, st);
     for (int i = 0; i < a->steps; ++i) {
         t.mark(0, st);
-        bm::launch_prologue(s, P.external_tool ? 0 : 1, st);
+        bm::launch_prologue(s, P.external_tool ? 0 : 1, st, force_topology ? 1 : 0);
         t.mark(1, st);
         bm::launch_rigid(s, a->cut_bits, st);
         t.mark(2, st);
@@ -92,7 +107,7 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         }
         bm::launch_pairs(s, st);
         t.mark(3, st);
-        bm::launch_register(s, field_codes, P.cache_topology ? 0 : 1, st);
+        bm::launch_register(s, field_codes, force_topology ? 1 : 0, st, 0);
         t.mark(4, st);
         bm::launch_material(s, 0, st);
         if (P.external_tool && !P.predict) bm::launch_hold(s, st);
@@ -184,7 +199,8 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     s->B = *buffers;
     s->buckets = (int64_t)P.bucket_mask + 1;
     layout_scratch(s);
-    if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaMemset(bm::scan_ticket(s->B), 0, sizeof(int32_t)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess) {
         delete s;
@@ -370,7 +386,8 @@ int bm_batch_graph_create(bm_solver* const* solvers, const bm_step_args* args, i
     cudaEventRecord(start, origin);
     for (int l = 0; l < lanes; ++l) cudaStreamWaitEvent(lane[l], start, 0);
     int rc = BM_OK;
-    for (int i = 0; i < count && rc == BM_OK; ++i) rc = run_batch(solvers[i], &args[i], lane[i % lanes]);
+    for (int i = 0; i < count && rc == BM_OK; ++i)
+        rc = run_batch(solvers[i], &args[i], lane[i % lanes]);
     for (int l = 0; l < lanes; ++l) {
         cudaEventRecord(done[l], lane[l]);
         cudaStreamWaitEvent(origin, done[l], 0);
@@ -415,16 +432,8 @@ int bm_graph_destroy(bm_graph* g) {
 
 int bm_graph_kernel_count(const bm_graph* g, int64_t* count) {
     if (!g || !count) return fail(BM_ERR_ARGUMENT, "null argument");
-    size_t n = 0;
-    if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return check_cuda("graph nodes");
-    std::vector<cudaGraphNode_t> nodes(n);
-    if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return check_cuda("graph nodes");
-    int64_t kernels = 0;
-    for (size_t i = 0; i < n; ++i) {
-        cudaGraphNodeType type;
-        if (cudaGraphNodeGetType(nodes[i], &type) != cudaSuccess) return check_cuda("graph node type");
-        if (type == cudaGraphNodeTypeKernel) ++kernels;
-    }
+    const int64_t kernels = kernel_nodes(g->graph);
+    if (kernels < 0) return check_cuda("graph nodes");
     *count = kernels;
     return BM_OK;
 }

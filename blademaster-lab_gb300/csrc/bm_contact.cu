@@ -446,8 +446,13 @@ __device__ __forceinline__ int list_bucket(int cx, int cy, int cz, int mask) {
 }
 
 // Solver prologue of a substep: clear_pair_slots (contact.py:643-652) of the
-// table written this substep, and clear_step (contact.py:1058-1068).
-__global__ void k_prologue(bm_params P, bm_buffers B, int clear_step) {
+// table written this substep, and clear_step (contact.py:1058-1068).  It
+// also opens the substep's gated work, whose flags are final by now: the
+// largest-displacement bound of a full pair-list build (reset when the list
+// is rebuilt this substep), and with registration >= 0 the counters of a
+// topology registration (when the topology is dirty, or always with
+// registration == 1), which the registration kernels then fill.
+__global__ void k_prologue(bm_params P, bm_buffers B, int clear_step, int registration) {
     const int step = B.flags[BM_FLAG_STEP];
     const int nw = (step + 1) & 1;
     const int64_t cap = P.pair_capacity;
@@ -463,44 +468,48 @@ __global__ void k_prologue(bm_params P, bm_buffers B, int clear_step) {
         }
         if (threadIdx.x == 0) B.speed[0] = 0.0f;
     }
+    if (threadIdx.x == 0) {
+        if (P.pair_search != 0 || B.flags[BM_FLAG_PAIR_DIRTY] != 0) B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f
+        if (registration == 1 || (registration == 0 && B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0)) {
+            B.flags[BM_FLAG_MULTI] = 0;
+            B.flags[BM_FLAG_MIXED_CELLS] = 0;
+            B.flags[BM_FLAG_REGISTRATIONS] += 1;
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0) B.pair_count[nw] = 0;
 }
 
+// First kernel of a full pair-list build.  Block 0 does
 // contact.set_pair_reach (contact.py:748-761) for the list search, or the
-// hash search reach 2 radius + 2 dt speed (contact.py:684); resets the build.
-__global__ void k_pair_setup(bm_params P, bm_buffers B, float* reach_out, int force) {
-    if (!force && B.flags[BM_FLAG_PAIR_DIRTY] == 0) return;
-    const float speed = B.speed[0];
-    float value;
-    if (P.pair_search == 0) {
-        value = 2.0f * P.radius + P.pair_skin;
-        if (P.dt * speed > 0.5f * P.pair_skin) value += 2.0f * P.dt * speed;
-    } else {
-        value = 2.0f * P.radius + 2.0f * speed * P.dt;
-    }
-    *reach_out = value;
-    B.flags[BM_FLAG_CANDIDATES] = 0;
-    B.flags[BM_FLAG_PAIR_BUILDS] += 1;
-    B.flags[BM_FLAG_CHANGED] = 0;  // a full build uses the current codes
-    B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f, raised by k_max_disp
-}
-
-// Largest displacement |x - ref| over all particles, for the build's
-// reference-distance bound (see build_list).
-__global__ void k_max_disp(bm_params P, bm_buffers B, const int32_t* gate_flag) {
+// hash search reach 2 radius + 2 dt speed (contact.py:684), and resets the
+// build's counters; every block zeroes bucket counts and raises the largest
+// displacement |x - ref| over all particles (the build's reference-distance
+// bound, see build_list; k_prologue reset it).
+__global__ void k_pair_begin(bm_params P, bm_buffers B, float* reach_out, int64_t buckets, const int32_t* gate_flag) {
     if (gate_flag && *gate_flag == 0) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const float speed = B.speed[0];
+        float value;
+        if (P.pair_search == 0) {
+            value = 2.0f * P.radius + P.pair_skin;
+            if (P.dt * speed > 0.5f * P.pair_skin) value += 2.0f * P.dt * speed;
+        } else {
+            value = 2.0f * P.radius + 2.0f * speed * P.dt;
+        }
+        *reach_out = value;
+        B.flags[BM_FLAG_CANDIDATES] = 0;
+        B.flags[BM_FLAG_PAIR_BUILDS] += 1;
+        B.flags[BM_FLAG_CHANGED] = 0;  // a full build uses the current codes
+    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < buckets; i += stride) B.bucket_fill[i] = 0;
     const int N = P.n;
     float d = 0.0f;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
         d = fmaxf(d, v3_len(v3_sub(ld3(B.x, N, p), ld3(B.ref, N, p))));
     for (int s = 16; s > 0; s >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, s));
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_MAX_DISP]), d);
-}
-
-__global__ void k_zero_i32(int32_t* a, int64_t n, const int32_t* gate_flag) {
-    if (gate_flag && *gate_flag == 0) return;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = 0;
 }
 
 __global__ void k_bin_count(bm_params P, bm_buffers B, const float* reach_in, const int32_t* gate_flag) {
@@ -533,11 +542,34 @@ __device__ __forceinline__ int32_t block_scan_1024(int32_t v, int32_t* s) {
     return r;
 }
 
+// Exclusive scan of the tile sums (one block of 1024 threads); the total of
+// all tiles goes to *total_out.  The sums are read through L2: other blocks
+// of the same kernel wrote them.
+__device__ void scan_partials_block(int32_t* partials, int64_t tiles, int32_t* total_out) {
+    __shared__ int32_t s[1024];
+    const int64_t chunk = (tiles + 1023) / 1024;
+    const int64_t begin = threadIdx.x * chunk, end = min(begin + chunk, tiles);
+    int32_t sum = 0;
+    for (int64_t i = begin; i < end; ++i) sum += __ldcg(partials + i);
+    const int32_t inc = block_scan_1024(sum, s);
+    int32_t run = inc - sum;
+    for (int64_t i = begin; i < end; ++i) {
+        const int32_t v = __ldcg(partials + i);
+        partials[i] = run;
+        run += v;
+    }
+    if (threadIdx.x == 1023 && total_out) *total_out = inc;
+}
+
 // Exclusive scan of `count` ints: tiles of 1024 (grid-stride over tiles),
-// a one-block scan of the tile sums, then the tile offsets added.
-__global__ void k_scan_tiles(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, const int32_t* gate_flag) {
+// then the block that finishes last (a ticket counter; no block waits)
+// scans the tile sums and resets the ticket; k_scan_add adds the tile
+// offsets.
+__global__ void k_scan_tiles(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, int32_t* total_out,
+                             int32_t* ticket, const int32_t* gate_flag) {
     if (gate_flag && *gate_flag == 0) return;
     __shared__ int32_t s[1024];
+    __shared__ int last;
     const int64_t tiles = (count + 1023) / 1024;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int64_t i = tile * 1024 + threadIdx.x;
@@ -546,22 +578,17 @@ __global__ void k_scan_tiles(const int32_t* in, int32_t* out, int64_t count, int
         if (i < count) out[i] = inc - v;
         if (threadIdx.x == 1023) partials[tile] = inc;
     }
-}
-__global__ void k_scan_partials(int32_t* partials, int64_t tiles, int32_t* total_out, const int32_t* gate_flag) {
-    if (gate_flag && *gate_flag == 0) return;
-    __shared__ int32_t s[1024];
-    const int64_t chunk = (tiles + 1023) / 1024;
-    const int64_t begin = threadIdx.x * chunk, end = min(begin + chunk, tiles);
-    int32_t sum = 0;
-    for (int64_t i = begin; i < end; ++i) sum += partials[i];
-    const int32_t inc = block_scan_1024(sum, s);
-    int32_t run = inc - sum;
-    for (int64_t i = begin; i < end; ++i) {
-        const int32_t v = partials[i];
-        partials[i] = run;
-        run += v;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
     }
-    if (threadIdx.x == 1023 && total_out) *total_out = inc;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    scan_partials_block(partials, tiles, total_out);
+    if (threadIdx.x == 0) *ticket = 0;
 }
 __global__ void k_scan_add(int32_t* out, int64_t count, const int32_t* partials, const int32_t* gate_flag) {
     if (gate_flag && *gate_flag == 0) return;
@@ -656,8 +683,12 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
 // buckets), so their lists are recomputed with the new codes.  Codes only
 // gain digits, so compatibility only turns false and lists only grow; the
 // positions are still within half a skin of the build (else a full build ran).
-__global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in) {
+__global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in, int clear_dirty) {
     const int changed = min(B.flags[BM_FLAG_CHANGED], P.n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (clear_dirty) B.flags[BM_FLAG_PAIR_DIRTY] = 0;  // any full build ran before this kernel
+        if (changed != 0) B.flags[BM_FLAG_RELISTS] += 1;
+    }
     if (changed == 0) return;
     const int N = P.n;
     const float reach = *reach_in;
@@ -693,15 +724,15 @@ __global__ void k_relist(bm_params P, bm_buffers B, const float* reach_in) {
     }
 }
 
-__global__ void k_relist_done(bm_buffers B) {
-    B.flags[BM_FLAG_CHANGED] = 0;
-    B.flags[BM_FLAG_RELIST] = 0;
-}
-
 // contact.pairs_listed (contact.py:825-925): each candidate adds its pair
-// impulses to its rigid impulse in ascending partner order.
+// impulses to its rigid impulse in ascending partner order.  The lists are
+// current by now, so the changed-code and relist counts are reset here.
 __global__ void k_pairs(bm_params P, bm_buffers B, const float* reach_in) {
     const int candidates = min(B.flags[BM_FLAG_CANDIDATES], P.candidate_capacity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        B.flags[BM_FLAG_CHANGED] = 0;
+        B.flags[BM_FLAG_RELIST] = 0;
+    }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < candidates; t += gridDim.x * blockDim.x)
         pair_particle(P, B, B.candidates[t], *reach_in);
 }
@@ -830,8 +861,8 @@ __global__ void k_resist_cut(const float* j, const float* x, const float* v, con
 
 // --------------------------------------------------------------- launches
 
-void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st) {
-    k_prologue<<<1, 1024, 0, st>>>(s->P, s->B, clear_step);
+void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st, int registration) {
+    k_prologue<<<1, 1024, 0, st>>>(s->P, s->B, clear_step, registration);
 }
 
 void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st) {
@@ -841,10 +872,16 @@ void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st) {
 void launch_pairs(const bm_solver* s, cudaStream_t st) { launch_pairs_using(s, s->scan_partials, st); }
 
 void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) {
+    const int force = s->P.pair_search != 0;
+    launch_pair_build(s, partials, !force, st);
+    if (!force) launch_relist(s, 1, st);
+    launch_pair_impulses(s, st);
+}
+
+void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, cudaStream_t st) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
-    const int force = P.pair_search != 0;
-    const int32_t* gate = force ? nullptr : &B.flags[BM_FLAG_PAIR_DIRTY];
+    const int32_t* gate = gated ? &B.flags[BM_FLAG_PAIR_DIRTY] : nullptr;
     float* reach = reinterpret_cast<float*>(B.scratch);
     const int64_t buckets = s->buckets;
     const int64_t tiles = (buckets + 1023) / 1024;
@@ -852,32 +889,34 @@ void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) 
     const unsigned gb = grid_for(buckets) < wide ? grid_for(buckets) : wide;
     const unsigned gn = grid_for(P.n) < wide ? grid_for(P.n) : wide;
     const unsigned gt = tiles < 152 ? (unsigned)tiles : 152;
-    k_pair_setup<<<1, 1, 0, st>>>(P, B, reach, force);
-    k_max_disp<<<gn, kBlock, 0, st>>>(P, B, gate);
-    k_zero_i32<<<gb, kBlock, 0, st>>>(B.bucket_fill, buckets, gate);
+    k_pair_begin<<<gn > gb ? gn : gb, kBlock, 0, st>>>(P, B, reach, buckets, gate);
     k_bin_count<<<gn, kBlock, 0, st>>>(P, B, reach, gate);
-    k_scan_tiles<<<gt, 1024, 0, st>>>(B.bucket_fill, B.bucket_start, buckets, partials, gate);
-    k_scan_partials<<<1, 1024, 0, st>>>(partials, tiles, B.bucket_start + buckets, gate);
+    k_scan_tiles<<<gt, 1024, 0, st>>>(B.bucket_fill, B.bucket_start, buckets, partials, B.bucket_start + buckets,
+                                      scan_ticket(B), gate);
     k_scan_add<<<gb, kBlock, 0, st>>>(B.bucket_start, buckets, partials, gate);
     k_bin_scatter<<<gn, kBlock, 0, st>>>(P, B, gate);
     k_build_lists<<<gn, kBlock, 0, st>>>(P, B, reach, gate);
-    if (!force) {
-        launch_clear_flag(s, BM_FLAG_PAIR_DIRTY, st);
-        k_relist_mark<<<152, kBlock, 0, st>>>(P, B, reach);
-        k_relist<<<152, kBlock, 0, st>>>(P, B, reach);
-        k_relist_done<<<1, 1, 0, st>>>(B);
-    }
+}
+
+void launch_relist(const bm_solver* s, int clear_dirty, cudaStream_t st) {
+    float* reach = reinterpret_cast<float*>(s->B.scratch);
+    k_relist_mark<<<152, kBlock, 0, st>>>(s->P, s->B, reach, clear_dirty);
+    k_relist<<<152, kBlock, 0, st>>>(s->P, s->B, reach);
+}
+
+void launch_pair_impulses(const bm_solver* s, cudaStream_t st) {
+    const bm_params& P = s->P;
+    const unsigned wide = 4 * 152;
     const unsigned gc = grid_for(P.candidate_capacity) < wide ? grid_for(P.candidate_capacity) : wide;
-    k_pairs<<<gc, kBlock, 0, st>>>(P, B, reach);
+    k_pairs<<<gc, kBlock, 0, st>>>(P, s->B, reinterpret_cast<float*>(s->B.scratch));
 }
 
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, int32_t* total_out,
-                           const int32_t* gate, cudaStream_t st) {
+                           int32_t* ticket, const int32_t* gate, cudaStream_t st) {
     const int64_t tiles = (count + 1023) / 1024;
     const unsigned gt = tiles < 152 ? (unsigned)(tiles < 1 ? 1 : tiles) : 152;
     const unsigned ga = grid_for(count) < 4 * 152 ? grid_for(count) : 4 * 152;
-    k_scan_tiles<<<gt, 1024, 0, st>>>(in, out, count, partials, gate);
-    k_scan_partials<<<1, 1024, 0, st>>>(partials, tiles, total_out, gate);
+    k_scan_tiles<<<gt, 1024, 0, st>>>(in, out, count, partials, total_out, ticket, gate);
     k_scan_add<<<ga, kBlock, 0, st>>>(out, count, partials, gate);
 }
 

@@ -24,7 +24,8 @@ struct bm_graph {
 namespace bm {
 
 // material
-void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st);
+// begin == 0: k_prologue of the same substep already began the registration.
+void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st, int begin = 1);
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st);
 void launch_g2p(const bm_solver* s, cudaStream_t st);
 void launch_remap(const bm_solver* s, cudaStream_t st);
@@ -36,18 +37,30 @@ void launch_clear_flag(const bm_solver* s, int which, cudaStream_t st);
 void launch_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, cudaStream_t st);
 
 // contact
-void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st);
+// With registration >= 0 the prologue also begins a topology registration
+// (always with 1, when the topology is dirty with 0) for a launch_register
+// with begin == 0 later in the substep.
+void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st, int registration = -1);
 void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st);
 void launch_pairs(const bm_solver* s, cudaStream_t st);
 // The same launches with the bucket-scan partials (one int per 1024 buckets,
 // written before they are read) at `partials`.
 void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st);
+// The three parts of launch_pairs: the full pair-list build (each kernel
+// returns at once unless flags[BM_FLAG_PAIR_DIRTY] is set, when `gated`),
+// the incremental relist of particles near changed codes (clearing
+// flags[BM_FLAG_PAIR_DIRTY] too, when `clear_dirty`), and the pair impulses.
+void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, cudaStream_t st);
+void launch_relist(const bm_solver* s, int clear_dirty, cudaStream_t st);
+void launch_pair_impulses(const bm_solver* s, cudaStream_t st);
 void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st);
 // Exclusive prefix sum of `count` ints (one int of `partials` per 1024 of
 // them); the total goes to *total_out.  Every kernel returns at once when
 // `gate` is non-null and *gate == 0.
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int64_t count, int32_t* partials, int32_t* total_out,
-                           const int32_t* gate, cudaStream_t st);
+                           int32_t* ticket, const int32_t* gate, cudaStream_t st);
+// Scratch word 1: the ticket of the scans' last-block pass (zero between scans).
+inline int32_t* scan_ticket(const bm_buffers& B) { return B.scratch + 1; }
 
 // held-blade constraint (external tool in hold mode)
 void launch_hold(const bm_solver* s, cudaStream_t st);

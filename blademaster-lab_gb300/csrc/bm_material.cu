@@ -1168,14 +1168,14 @@ __global__ void k_grid_vel(bm_params P, bm_buffers B, const float* __restrict__ 
 
 // --------------------------------------------------------------- launches
 
-void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st) {
+void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st, int begin) {
     const bm_params& P = s->P;
     const unsigned wide = 8 * 152;  // grid-stride: cheap to launch when the gate is off
     const unsigned gn = grid_for(P.active_nodes) < wide ? grid_for(P.active_nodes) : wide;
     const unsigned gp = grid_for(P.n) < wide ? grid_for(P.n) : wide;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     const unsigned gc = grid_for(cells8) < wide ? grid_for(cells8) : wide;
-    k_register_begin<<<1, 1, 0, st>>>(s->B, force);
+    if (begin) k_register_begin<<<1, 1, 0, st>>>(s->B, force);
     k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes, force);
     k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes, force);
     k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B, force);

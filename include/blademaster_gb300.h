@@ -202,6 +202,7 @@ typedef struct bm_buffers {
 #define BM_FLAG_CHANGED 7        /* entries of buffers.changed */
 #define BM_FLAG_RELIST 8         /* entries of buffers.relist_list */
 #define BM_FLAG_MULTI 9          /* entries of buffers.multi_nodes */
+#define BM_FLAG_RELISTS 10       /* incremental pair-list updates run (codes changed, no full build) */
 /* word 10 is unused */
 #define BM_FLAG_MIXED_CELLS 11   /* entries of buffers.mixed_cells */
 #define BM_FLAG_REGISTRATIONS 12 /* topology registrations run */

@@ -101,6 +101,32 @@ def test_graph_replay_is_bitexact_with_eager_and_oracle():
         np.testing.assert_array_equal(graphed.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
 
 
+@pytest.mark.parametrize("cache_topology", [False, True])
+def test_gated_chains_in_graphs_match_eager_launches(cache_topology):
+    """The full pair-list build, the incremental relist and (with a cached
+    topology) the registration are gated on device flags; a replayed graph
+    and eager launches run each of them equally often, with equal results."""
+    from blademaster_gb300 import _native
+
+    cfg = replace(Config(), cache_topology=cache_topology)
+    eager, graphed = Solver(cfg), Solver(cfg)
+    for s in (eager, graphed):
+        s.tool_pos.assign([[0.0, 0.0, 0.047]])
+    edges = np.stack([np.zeros(48), np.zeros(48), np.linspace(0.044, 0.030, 48)], axis=1)
+    for begin in range(0, 48, 8):
+        eager.advance(edges[begin:begin + 8], True, 0, graph=False)
+        graphed.advance(edges[begin:begin + 8], True, 0, graph=True)
+        for name in EXACT + ("Fp", "impulses"):
+            np.testing.assert_array_equal(getattr(eager, name).numpy(), getattr(graphed, name).numpy(), err_msg=name)
+    ef, gf = eager._t["flags"].cpu().numpy(), graphed._t["flags"].cpu().numpy()
+    for name in ("PAIR_BUILDS", "RELISTS", "REGISTRATIONS", "PAIR_DIRTY", "TOPOLOGY_DIRTY", "CANDIDATES", "MULTI",
+                 "MIXED_CELLS", "MAX_DISP"):
+        assert ef[_native.FLAG[name]] == gf[_native.FLAG[name]], name
+    assert gf[_native.FLAG["PAIR_BUILDS"]] >= 2 and gf[_native.FLAG["RELISTS"]] >= 1
+    assert gf[_native.FLAG["REGISTRATIONS"]] >= (2 if cache_topology else 48)
+    assert np.count_nonzero(graphed.codes.numpy()) > 0
+
+
 def test_external_interval_matches_oracle():
     cfg = replace(Config(), external_tool=True)
     g, c = both(cfg)
