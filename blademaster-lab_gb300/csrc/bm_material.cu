@@ -309,47 +309,33 @@ __device__ void emit_runs(const bm_params& P, const bm_buffers& B, const float (
     if (s == 0) B.mixed_run[node * 8 + a] = (at << 4) | k;
 }
 
-// Mixed-cell pass of p2g: 8 lanes per listed cell (warp-uniform loop).
+// Mixed-cell pass of p2g: 8 lanes per (listed cell, corner), so the 64
+// threads of a cell are two whole warps and every warp handles one cell.
 __global__ void __launch_bounds__(256) k_p2g_mixed_cells(bm_params P, bm_buffers B) {
-    const int listed = B.flags[BM_FLAG_MIXED_CELLS];
+    const int64_t threads = 64 * (int64_t)B.flags[BM_FLAG_MIXED_CELLS];
     const int N = P.n;
-    const int stride = gridDim.x * blockDim.x;
-    for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * listed; t0 += stride) {
-        const int t = t0 + threadIdx.x;
-        const int j = t >> 3, s = t & 7;
-        const bool valid = j < listed;
-        const unsigned gmask = 0xffu << (threadIdx.x & 24);
-        if (!__any_sync(kFull, valid)) break;
-        if (!valid) continue;  // whole groups only: the group is valid or not
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < threads; t += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(t >> 6), a = (int)(t >> 3) & 7, s = (int)t & 7;
         const int c = B.mixed_cells[j];
         const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
         const bool present = s < count;
-        const int p = b + s, base = cell_base_node(P, c);
-        bm_v3 v = v3_zero(), imp = v3_zero();
-        bm_m33 S = m33_zero();
-        int sid = 0;
-        uint64_t fidx = 0u;
+        const int p = b + s;
+        float vals[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        int f = kMixed;
         if (present) {
-            v = ld3(B.v, N, p);
-            imp = ld3(B.impulses, N, p);
-            S = m33_scale(ld9(B.stress, N, p), P.dt * P.volume);
-            sid = B.stencil_id[p];
-            fidx = B.fidx[p];
+            const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
+                                             m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
+            vals[0] = k.m;
+            vals[1] = k.mom.x;
+            vals[2] = k.mom.y;
+            vals[3] = k.mom.z;
+            vals[4] = k.J.x;
+            vals[5] = k.J.y;
+            vals[6] = k.J.z;
+            f = field_of(B.fidx[p], a);
         }
-        for (int a = 0; a < 8; ++a) {
-            float vals[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-            if (present) {
-                const P2GContrib k = p2g_contrib(P, B, v, imp, S, sid, a);
-                vals[0] = k.m;
-                vals[1] = k.mom.x;
-                vals[2] = k.mom.y;
-                vals[3] = k.mom.z;
-                vals[4] = k.J.x;
-                vals[5] = k.J.y;
-                vals[6] = k.J.z;
-            }
-            emit_runs<7>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask, (j * 8 + a) * 8);
-        }
+        emit_runs<7>(P, B, vals, a, f, cell_base_node(P, c), gmask, (j * 8 + a) * 8);
     }
 }
 
@@ -648,40 +634,28 @@ __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float ha
     }
 }
 
-// Mixed-cell pass of the re-scatter (new particle velocities).
+// Mixed-cell pass of the re-scatter (new particle velocities), 8 lanes per
+// (listed cell, corner) like k_p2g_mixed_cells.
 __global__ void __launch_bounds__(256) k_remap_mixed_cells(bm_params P, bm_buffers B) {
-    const int listed = B.flags[BM_FLAG_MIXED_CELLS];
+    const int64_t threads = 64 * (int64_t)B.flags[BM_FLAG_MIXED_CELLS];
     const int N = P.n;
-    const int stride = gridDim.x * blockDim.x;
-    for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * listed; t0 += stride) {
-        const int t = t0 + threadIdx.x;
-        const int j = t >> 3, s = t & 7;
-        const bool valid = j < listed;
-        const unsigned gmask = 0xffu << (threadIdx.x & 24);
-        if (!__any_sync(kFull, valid)) break;
-        if (!valid) continue;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < threads; t += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(t >> 6), a = (int)(t >> 3) & 7, s = (int)t & 7;
         const int c = B.mixed_cells[j];
         const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
         const bool present = s < count;
-        const int p = b + s, base = cell_base_node(P, c);
-        bm_v3 v = v3_zero();
-        int sid = 0;
-        uint64_t fidx = 0u;
+        const int p = b + s;
+        float vals[3] = {0.0f, 0.0f, 0.0f};
+        int f = kMixed;
         if (present) {
-            v = ld3(B.v, N, p);
-            sid = B.stencil_id[p];
-            fidx = B.fidx[p];
+            const bm_v3 r = v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a));
+            vals[0] = r.x;
+            vals[1] = r.y;
+            vals[2] = r.z;
+            f = field_of(B.fidx[p], a);
         }
-        for (int a = 0; a < 8; ++a) {
-            float vals[3] = {0.0f, 0.0f, 0.0f};
-            if (present) {
-                const bm_v3 r = v3_mul(v, P.mass * stencil_w(B, sid, a));
-                vals[0] = r.x;
-                vals[1] = r.y;
-                vals[2] = r.z;
-            }
-            emit_runs<3>(P, B, vals, a, present ? field_of(fidx, a) : kMixed, base, gmask, (j * 8 + a) * 8);
-        }
+        emit_runs<3>(P, B, vals, a, f, cell_base_node(P, c), gmask, (j * 8 + a) * 8);
     }
 }
 
@@ -1186,7 +1160,7 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     const bm_buffers& B = s->B;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
-    k_p2g_mixed_cells<<<2 * 152, kBlock, 0, st>>>(P, B);
+    k_p2g_mixed_cells<<<8 * 152, kBlock, 0, st>>>(P, B);
     k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
     k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
     if (P.viscous) {
@@ -1205,7 +1179,7 @@ void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     k_g2p<<<grid_for(cells8), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
-    k_remap_mixed_cells<<<2 * 152, kBlock, 0, st>>>(P, s->B);
+    k_remap_mixed_cells<<<8 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
 void launch_remap(const bm_solver* s, cudaStream_t st) {
