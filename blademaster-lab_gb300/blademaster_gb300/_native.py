@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -193,6 +193,8 @@ def _declare(lib):
         "bm_batch_graph_create": ([ctypes.POINTER(vp), ctypes.POINTER(StepArgs), i, i, vp, ctypes.POINTER(vp)], i),
         "bm_graph_destroy": ([vp], i),
         "bm_graph_kernel_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
+        "bm_metrics": ([vp, vp, vp], i),
+        "bm_components": ([vp, vp, vp, vp, vp, vp, vp], i),
         "bm_count_embedded": ([vp, i, vp], i),
         "bm_validate_interval": ([vp, vp], i),
         "bm_read_accumulators": ([vp, vp, vp, vp, vp, vp], i),

@@ -712,6 +712,35 @@ class Solver:
         self._write_targets([target_edge], [orientation if orientation is not None else [0.0, 0.0, 0.0, 1.0]])
         self._call("bm_drive_tool", 0, self._stream)
 
+    def components(self, codes=None):
+        """Piece label of every particle and the piece sizes, computed on the device.
+
+        topology.components (topology.py:17-57) of node_numpy, weight_numpy and
+        ``codes`` ((n,) in reference order; default the current cut codes): the
+        labels rank the pieces by their lowest particle index.  Returns int64
+        (labels (n,), sizes (pieces,)) like the reference.
+        """
+        import torch
+
+        n = self.n
+        if getattr(self, "_pieces", None) is None:
+            self._pieces = [torch.zeros(n, dtype=torch.int32, device=self.device) for _ in range(2)]
+            self._pieces.append(torch.zeros(1, dtype=torch.int32, device=self.device))
+        labels, sizes, count = self._pieces
+        code_ptr = None
+        if codes is not None:
+            codes = np.asarray(codes, np.int64)
+            if codes.shape != (n,):
+                raise ValueError(f"codes must have shape ({n},)")
+            device_codes = torch.as_tensor(codes, device=self.device).index_select(0, self._order_t)
+            code_ptr = device_codes.data_ptr()
+        self._call("bm_components", code_ptr, self._order_t.data_ptr(), labels.data_ptr(), sizes.data_ptr(),
+                   count.data_ptr(), self._stream)
+        pieces = int(count.item())
+        if pieces < 0:
+            raise RuntimeError("Piece labelling gave up (union retries exhausted)")
+        return labels.cpu().numpy().astype(np.int64), sizes[:pieces].cpu().numpy().astype(np.int64)
+
     def embedded_particles(self):
         """Number of particles beside the blade body; zero once the blade has left the material."""
         self._call("bm_count_embedded", 1, self._stream)

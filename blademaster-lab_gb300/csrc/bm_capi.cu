@@ -44,7 +44,8 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int64_t tiles_of(const bm_params& P) { return ((int64_t)P.bucket_mask + 1 + 1023) / 1024; }
 
 void layout_scratch(bm_solver* s) {
-    // [0] pair reach (float), [1] scan ticket, [64 .. 64 + tiles) scan partials, then 9 n floats (viscous stress).
+    // [0] pair reach (float), [1] scan ticket, [8, 25) observation sums and counters (zero between
+    // calls), [64 .. 64 + tiles) scan partials, then 9 n floats (viscous stress).
     int32_t* base = s->B.scratch;
     s->scan_partials = base + 64;
     int64_t off = 64 + tiles_of(s->P);
@@ -199,7 +200,7 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     s->B = *buffers;
     s->buckets = (int64_t)P.bucket_mask + 1;
     layout_scratch(s);
-    if (cudaMemset(bm::scan_ticket(s->B), 0, sizeof(int32_t)) != cudaSuccess ||
+    if (cudaMemset(s->B.scratch + 1, 0, 63 * sizeof(int32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess) {

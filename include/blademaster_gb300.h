@@ -298,6 +298,22 @@ int bm_batch_graph_create(bm_solver* const* solvers, const bm_step_args* args, i
                           bm_graph** out);
 /* Number of kernel launches one bm_graph_launch of `g` performs (its kernel nodes). */
 int bm_graph_kernel_count(const bm_graph* g, int64_t* count);
+/* diagnostics.Metrics.read (diagnostics.py:7-48) of the solver's state into
+ * out[6] (device, float64): kinetic, gravitational and elastic energy (J),
+ * largest speed (m/s), largest height z (m), smallest det F.  The sums are
+ * exact before their one rounding to float64, so they do not depend on the
+ * order of the particles; the extrema start from 0, -1e20 and 1e20. */
+int bm_metrics(bm_solver* s, double* out, void* stream);
+/* topology.components (topology.py:17-57) on the device.  codes: [n] cut
+ * codes in device particle order, or NULL for the solver's codes; order: [n]
+ * reference index of each device particle.  labels: [n] (by reference index)
+ * piece of each particle, pieces ranked by their lowest reference index;
+ * sizes: [n] particles per piece (the first *count entries); count: pieces,
+ * or -1 if a union gave up.  All device pointers; labels and sizes are also
+ * the workspace.  A stencil node joins a particle's piece when its float32
+ * weight is positive. */
+int bm_components(bm_solver* s, const int64_t* codes, const int64_t* order, int32_t* labels, int32_t* sizes,
+                  int32_t* count, void* stream);
 /* Stages of one substep, in launch order (profiling). */
 #define BM_STAGE_PROLOGUE 0  /* clear_pair_slots + clear_step */
 #define BM_STAGE_RIGID 1     /* rigid_and_speed + extra_blade */

@@ -1703,3 +1703,40 @@ ORC_API void orc_fx_roundtrip(const float* x, int n, double* out) {
     int i;
     for (i = 0; i < n; ++i) out[i] = bm_fx_to_double(bm_fx_from_float(x[i]));
 }
+
+/* diagnostics.metrics (diagnostics.py:7-32) of n particles (AoS): out[0..2]
+ * the exact 128-bit fixed-point sums of the kinetic, gravitational and
+ * elastic energies (one rounding to double), out[3] max |v| (from 0),
+ * out[4] max z (from -1e20), out[5] min det F (from 1e20).  The per-particle
+ * terms use the kernel's operation order, so the sums are bit-exact with the
+ * device's whatever the order of its atomic additions. */
+ORC_API void orc_metrics(const float* x, const float* v, const float* F, const float* Fp, int n, float mass,
+                         float volume, float mu, float lam, double* out) {
+    bm_fx sum[3];
+    float speed = 0.0f, top = -1.0e20f, low = 1.0e20f;
+    int i, a, b, k;
+    for (k = 0; k < 3; ++k) { sum[k].lo = 0u; sum[k].hi = 0u; }
+    for (i = 0; i < n; ++i) {
+        bm_v3 xp = ld3(x, i), vp = ld3(v, i), s;
+        bm_m33 f = ld9(F, i), fe = m33_mul(f, m33_inverse(ld9(Fp, i))), u, w, strain;
+        float energy = 0.0f, J, len, det;
+        bm_svd3(fe, &u, &s, &w);
+        strain = m33_sub(fe, m33_mul(u, m33_transpose(w)));
+        for (a = 0; a < 3; ++a)
+            for (b = 0; b < 3; ++b) energy = energy + mu * strain.m[a][b] * strain.m[a][b];
+        J = m33_det(fe);
+        energy = energy + 0.5f * lam * (J - 1.0f) * (J - 1.0f);
+        sum[0] = bm_fx_add(sum[0], bm_fx_from_float(0.5f * mass * v3_dot(vp, vp)));
+        sum[1] = bm_fx_add(sum[1], bm_fx_from_float(mass * 9.81f * xp.z));
+        sum[2] = bm_fx_add(sum[2], bm_fx_from_float(volume * energy));
+        len = v3_len(vp);
+        det = m33_det(f);
+        if (len > speed) speed = len;
+        if (xp.z > top) top = xp.z;
+        if (det < low) low = det;
+    }
+    for (k = 0; k < 3; ++k) out[k] = bm_fx_to_double(sum[k]);
+    out[3] = speed;
+    out[4] = top;
+    out[5] = low;
+}

@@ -104,7 +104,9 @@ def lib():
         L.orc_math_d.argtypes = [vp, vp, i, vp, vp, vp]
         L.orc_svd.argtypes = [vp, i, vp, vp, vp, vp]
         L.orc_fx_roundtrip.argtypes = [vp, i, vp]
-        for name in ("orc_couple_fields", "orc_g2p", "orc_math_f", "orc_math_d", "orc_svd", "orc_fx_roundtrip"):
+        L.orc_metrics.argtypes = [vp, vp, vp, vp, i, f, f, f, f, vp]
+        for name in ("orc_couple_fields", "orc_g2p", "orc_math_f", "orc_math_d", "orc_svd", "orc_fx_roundtrip",
+                     "orc_metrics"):
             getattr(L, name).restype = None
         L.orc_maxwell_hold.argtypes = [pp, ps, i]
         L.orc_maxwell_hold.restype = None
@@ -511,3 +513,13 @@ class MlsOracle:
         self.step_count += steps
         interval = self.contact["interval"]
         return interval[:3].copy(), interval[3:].copy()
+
+
+def metrics(x, v, F, Fp, mass, volume, mu, lam):
+    """diagnostics.metrics (diagnostics.py:7-32): the six values of Metrics.read as float64
+    (exact energy sums, then the extrema), in the device kernel's operation order."""
+    x, v = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (x, v))
+    F, Fp = (np.ascontiguousarray(a, np.float32).reshape(-1, 9) for a in (F, Fp))
+    out = np.zeros(6, np.float64)
+    lib().orc_metrics(ptr(x), ptr(v), ptr(F), ptr(Fp), len(x), mass, volume, mu, lam, ptr(out))
+    return out
