@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu", "bm_embed.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -91,7 +91,7 @@ def _struct_fields(name):
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
     fields = []
     for decl in body.split(";"):
-        decl = decl.strip()
+        decl = re.sub(r"^const\s+", "", decl.strip())
         if not decl:
             continue
         m = re.match(r"(\w+)\s*(\*?)\s*(.*)", decl)
@@ -128,6 +128,10 @@ class MlsParams(ctypes.Structure):
 
 class MlsBuffers(ctypes.Structure):
     _fields_ = _struct_fields("bm_mls_buffers")
+
+
+class Embedding(ctypes.Structure):
+    _fields_ = _struct_fields("bm_embedding")
 
 
 def header_constant(name):
@@ -195,6 +199,8 @@ def _declare(lib):
         "bm_graph_kernel_count": ([vp, ctypes.POINTER(ctypes.c_int64)], i),
         "bm_metrics": ([vp, vp, vp], i),
         "bm_components": ([vp, vp, vp, vp, vp, vp, vp], i),
+        "bm_embed_nodes": ([vp, vp, vp, vp, vp, ctypes.c_int64, i, vp, vp, vp, vp], i),
+        "bm_embed_vertices": ([vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
         "bm_count_embedded": ([vp, i, vp], i),
         "bm_validate_interval": ([vp, vp], i),
         "bm_read_accumulators": ([vp, vp, vp, vp, vp, vp], i),

@@ -314,6 +314,39 @@ int bm_metrics(bm_solver* s, double* out, void* stream);
  * weight is positive. */
 int bm_components(bm_solver* s, const int64_t* codes, const int64_t* order, int32_t* labels, int32_t* sizes,
                   int32_t* count, void* stream);
+/* Nodal embedding of a surface in the deformed material (surface.py:825-993,
+ * surface_gpu.py:11-345).  Reference nodes [node_count][3] and particle
+ * reference positions [particle_count][3]; the support of node i is
+ * indices/weights[offsets[i] .. offsets[i+1]) (tent weights, ascending
+ * particle ids), extra_* the second ring (tent radius 2 h).  Floating arrays
+ * hold doubles (scalar_bytes 8) or floats (4); all pointers are device
+ * pointers, F is [n][9] row-major. */
+typedef struct bm_embedding {
+    int32_t node_count, particle_count, scalar_bytes, pad;
+    const void* nodes;
+    const void* reference;
+    const int32_t* offsets;
+    const int32_t* indices;
+    const void* weights;
+    const int32_t* extra_offsets; /* may be NULL when extend == 0 */
+    const int32_t* extra_indices;
+    const void* extra_weights;
+} bm_embedding;
+/* MaterialEmbedding.field / node_state (surface.py:936-963): positions
+ * [node_count][3] and gradients [node_count][9] of each node's field for
+ * node_codes[i] (or `code` when node_codes is NULL); NaN where no compatible
+ * particle supports the node; with `extend` the second ring serves nodes the
+ * first cannot, and *extensions counts them (added to its value). */
+int bm_embed_nodes(const bm_embedding* e, const void* x, const void* F, const int64_t* codes,
+                   const int64_t* node_codes, int64_t code, int extend, void* positions, void* gradients,
+                   int32_t* extensions, void* stream);
+/* MaterialEmbedding.vertices through a material grid (surface_gpu.py:270-345):
+ * vertex v = sum_k corner_weights[v][k] * field(vertex_codes[v]) at node
+ * corners[v][k] (second ring allowed).  counts[0] += extended corner lookups,
+ * counts[1] += corners with weight > 1e-9 and no support (an error). */
+int bm_embed_vertices(const bm_embedding* e, int vertex_count, const int64_t* vertex_codes, const int32_t* corners,
+                      const void* corner_weights, const void* x, const void* F, const int64_t* codes, void* vertices,
+                      int32_t* counts, void* stream);
 /* Stages of one substep, in launch order (profiling). */
 #define BM_STAGE_PROLOGUE 0  /* clear_pair_slots + clear_step */
 #define BM_STAGE_RIGID 1     /* rigid_and_speed + extra_blade */
