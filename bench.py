@@ -89,6 +89,10 @@ STAGE_BYTES = {
     "remap": (20, 16),     # read v, field indices; read mass, write coupled velocity per slot
     "fupdate": (140, 16),  # read+write F, write stress, read x, v, code; read mass + coupled velocity per slot
 }
+# Stages that are one kernel each; the largest of them is the roofline's dominant kernel.
+SINGLE_KERNEL_STAGES = {"rigid": "k_rigid", "fupdate": "k_fupdate_assign"}
+# Whole-substep byte model: 296 B per particle, 156 B per slot (+108 B per particle with plasticity).
+SUBSTEP_BYTES = (296, 156)
 
 
 def sample_clocks(path):
@@ -377,11 +381,18 @@ def main():
     _native.check(s._lib.bm_substeps_profiled(s._handle, ctypes.byref(a), stage_ms, s._stream))
     s.step_count += args.profile_steps
     stages = {name: stage_ms[i] / args.profile_steps for i, name in enumerate(_native.STAGES)}
-    dominant = max(STAGE_BYTES, key=lambda k: stages[k])
+    dominant = max(SINGLE_KERNEL_STAGES, key=lambda k: stages[k])
     per_particle, per_slot = STAGE_BYTES[dominant]
     algo = per_particle * s.n + per_slot * slots
     achieved = algo / (stages[dominant] * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    stage_rooflines = {}
+    for name, (bp, bs) in STAGE_BYTES.items():
+        rate = (bp * s.n + bs * slots) / (stages[name] * 1e-3) / 1e9
+        stage_rooflines[name] = {"achieved_gbs": round(rate, 1), "frac": round(rate / peak, 4),
+                                 "traffic": traffic_per_launch(name, s.n, slots)}
+    substep_bytes = SUBSTEP_BYTES[0] * s.n + SUBSTEP_BYTES[1] * slots
+    substep_rate = substep_bytes / (ms / args.steps * 1e-3) / 1e9
 
     # end to end through the public API: H2D target, one substep, D2H knife state
     pinned_target = torch.zeros((1, 3), dtype=torch.float32).pin_memory()
@@ -426,7 +437,7 @@ def main():
         "gpu_launches": None,
         "stage_ms": {k: round(v, 5) for k, v in stages.items()},
         "roofline": {
-            "kernel": dominant,
+            "kernel": SINGLE_KERNEL_STAGES[dominant],
             "bound": "hbm",
             "achieved": achieved,
             "peak": peak,
@@ -436,6 +447,9 @@ def main():
             "algorithmic_bytes": algo,
             "traffic": traffic_per_launch(dominant, s.n, slots),
         },
+        "stage_rooflines": stage_rooflines,
+        "substep_roofline": {"algorithmic_bytes": substep_bytes, "achieved_gbs": round(substep_rate, 1),
+                             "frac": round(substep_rate / peak, 4)},
         "e2e": {
             "value": e2e_value,
             "unit": UNIT,
