@@ -87,10 +87,11 @@ STAGE_BYTES = {
     "p2g": (68, 28),       # read v, impulse, stress, code; write mass, old_v, new_v per slot
     "g2p": (56, 24),       # read+write x, v; read field indices; read old_v, new_v per slot
     "remap": (20, 16),     # read v, field indices; read mass, write coupled velocity per slot
-    "fupdate": (140, 16),  # read+write F, write stress, read x, v, code; read mass + coupled velocity per slot
+    "fupdate": (124, 12),  # read+write F, write stress, read stencil id, base node, field indices; coupled velocity per slot
+    "assign": (12, 0),     # read x (v and codes only for particles in a knife's band, not counted)
 }
 # Stages that are one kernel each; the largest of them is the roofline's dominant kernel.
-SINGLE_KERNEL_STAGES = {"rigid": "k_rigid", "fupdate": "k_fupdate_assign"}
+SINGLE_KERNEL_STAGES = {"rigid": "k_rigid", "fupdate": "k_fupdate", "assign": "k_assign"}
 # Whole-substep byte model: 296 B per particle, 156 B per slot (+108 B per particle with plasticity).
 SUBSTEP_BYTES = (296, 156)
 

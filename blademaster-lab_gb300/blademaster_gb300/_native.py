@@ -150,7 +150,7 @@ FLAG = {
               "HOLD_RESIDUAL", "HOLD_COUNT", "HOLD_NODES", "WORDS")
 }
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
-STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate"]
+STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate", "assign"]
 ACC_WORDS = 2 * (6 * MAX_TOOLS + 4)
 
 

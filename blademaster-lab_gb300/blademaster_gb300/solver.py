@@ -274,9 +274,6 @@ class Solver:
             T[name] = zeros(3, S)
         T["cell_part"] = zeros(7, 8, self.node_count)
         T["cell_field"] = t.as_tensor(np.ascontiguousarray(self._absent_corners(cell_start).T), device=dev)
-        T["mixed_run"] = t.full((self.node_count, 8), -1, dtype=i32, device=dev)
-        self.mixed_capacity = 8 * self.node_count
-        T["mixed_part"] = zeros(self.mixed_capacity, 8)
         T["multi_nodes"] = zeros(len(active), dtype=i32)
         T["mixed_cells"] = zeros(int(np.prod(cells)), dtype=i32)
         T["hist_mask"] = t.full((n,), -1, dtype=t.int16, device=dev)
@@ -381,7 +378,6 @@ class Solver:
         P.pair_capacity = self.pair_capacity
         P.bucket_mask = self.buckets - 1
         P.candidate_capacity = self.n
-        P.mixed_capacity = self.mixed_capacity
         P.tool_model = self._tool_model()
         P.external_tool = int(cfg.external_tool)
         P.predict = int(cfg.tool_substep == "predict")

@@ -120,8 +120,10 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         if (fork) cudaStreamWaitEvent(st, s->join, 0);
         else bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
         t.mark(8, st);
-        bm::launch_fupdate_assign(s, 1, a->cut_index, a->cut_bits != 0, 1, st);
+        bm::launch_fupdate(s, 1, 1, st);
         t.mark(9, st);
+        bm::launch_assign(s, a->cut_index, a->cut_bits != 0, st);
+        t.mark(10, st);
         if (t.on) {
             if (cudaEventSynchronize(t.ev[BM_STAGES]) != cudaSuccess) return check_cuda("profiled substep");
             for (int k = 0; k < BM_STAGES; ++k) {
@@ -183,7 +185,7 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
                               buffers->targets, buffers->rotations, buffers->packed, buffers->result,
                               buffers->scratch, buffers->cell_part, buffers->cell_field, buffers->hist_mask,
                               buffers->changed, buffers->relist, buffers->relist_list, buffers->listed,
-                              buffers->mixed_run, buffers->mixed_part, buffers->multi_nodes, buffers->mixed_cells,
+                              buffers->multi_nodes, buffers->mixed_cells,
                               buffers->particle_key, buffers->bucket_key, buffers->bucket_pos};
     for (const void* ptr : required)
         if (!ptr) return fail(BM_ERR_ARGUMENT, "a required buffer is null");
@@ -243,7 +245,7 @@ int bm_material_step(bm_solver* s, int single_field, void* stream) {
     if (s->P.external_tool && !s->P.predict) bm::launch_hold(s, st);
     bm::launch_g2p(s, st);
     bm::launch_remap(s, st);
-    bm::launch_fupdate_assign(s, 1, 0, 0, 0, st);
+    bm::launch_fupdate(s, 1, 0, st);
     return check_cuda("material_step");
 }
 
@@ -270,7 +272,7 @@ int bm_particle_contacts(bm_solver* s, void* stream) {
 
 int bm_assign_sides(bm_solver* s, int cut_index, int cutting, void* stream) {
     if (!s) return fail(BM_ERR_ARGUMENT, "null solver");
-    bm::launch_fupdate_assign(s, 0, cut_index, cutting, 0, as_stream(stream));
+    bm::launch_assign(s, cut_index, cutting, as_stream(stream));
     return check_cuda("assign_sides");
 }
 

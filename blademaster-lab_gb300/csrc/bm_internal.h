@@ -29,8 +29,10 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
 void launch_material(const bm_solver* s, int write_sums, cudaStream_t st);
 void launch_g2p(const bm_solver* s, cudaStream_t st);
 void launch_remap(const bm_solver* s, cudaStream_t st);
-void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,
-                           cudaStream_t st);
+// update_F + stress (do_update) and the substep counter (advance_step).
+void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st);
+// contact.assign for every knife (nothing when cutting == 0).
+void launch_assign(const bm_solver* s, int cut_index, int cutting, cudaStream_t st);
 void launch_refresh_stress(const bm_solver* s, cudaStream_t st);
 void launch_validate(const bm_solver* s, cudaStream_t st);
 void launch_clear_flag(const bm_solver* s, int which, cudaStream_t st);

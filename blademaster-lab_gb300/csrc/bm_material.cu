@@ -107,10 +107,10 @@ __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 // The corner flags (cell_field[node][a]: the field of a uniform corner, 255
 // when the cell's particles map to different fields there, 254 when there is
 // no cell) depend only on the field indices, so registration writes them and
-// lists the cells with a mixed corner.  Per substep, the cell pass writes one
-// partial per corner; the mixed-cell pass writes, for each mixed corner, one
-// partial per field present (a "run"); single-field nodes read eight
-// partials, multi-field nodes are handled one warp each.
+// counts the cells with a mixed corner.  Per substep, the cell pass writes one
+// partial per corner; single-field nodes read eight partials; multi-field
+// nodes are handled one warp each and sum a mixed corner's particles of each
+// field by the same tree straight from the cell's particles.
 
 constexpr int kMixed = 255;
 constexpr int kAbsent = 254;
@@ -263,131 +263,60 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     }
 }
 
-// Per-field tree sums of the mixed corners of one cell (8 lanes, mask gmask),
-// written to mixed_part as one run per corner (ascending field, at most 8
-// fields) in the fixed region of 8 entries that starts at `region`, and
-// recorded in mixed_run[node][a] (-1 when the region lies beyond the buffer:
-// the node pass then recomputes that corner).  Fixed regions need no shared
-// counter, so no atomic serialises the cells.
+// The V values at corner a of slot s of the cell whose particles are
+// [b, b + count): P2G sums (V = 7) or re-scatter momenta (V = 3) of a
+// particle with field f there, else +0.
 template <int V>
-__device__ void emit_runs(const bm_params& P, const bm_buffers& B, const float (&vals)[V], int a, int f, int base,
-                          unsigned gmask, int region) {
-    const int s = threadIdx.x & 7;
-    int lo = f, hi = f == kMixed ? -1 : f;
-    for (int d = 1; d < 8; d <<= 1) {
-        lo = min(lo, __shfl_xor_sync(gmask, lo, d));
-        hi = max(hi, __shfl_xor_sync(gmask, hi, d));
-    }
-    if (lo == hi) return;
-    const int at = region;
-    const int node = base + node_offset(P, a);
-    if (at + 8 > P.mixed_capacity) {
-        if (s == 0) B.mixed_run[node * 8 + a] = -1;
-        return;
-    }
-    int k = 0;
-    for (int cur = lo; cur != kMixed; ++k) {
-        float out[V];
+__device__ __forceinline__ void slot_value(const bm_params& P, const bm_buffers& B, int b, int count, int s, int a,
+                                           int f, float (&e)[V], bool& any) {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-            float x = f == cur ? vals[v] : 0.0f;
-            x = x + __shfl_xor_sync(gmask, x, 1);
-            x = x + __shfl_xor_sync(gmask, x, 2);
-            x = x + __shfl_xor_sync(gmask, x, 4);
-            out[v] = x;
-        }
-        if (s == 0) {
-            float* e = B.mixed_part + 8 * (at + k);
+    for (int v = 0; v < V; ++v) e[v] = 0.0f;
+    if (s >= count) return;
+    const int p = b + s;
+    if (field_of(B.fidx[p], a) != f) return;
+    any = true;
+    const int N = P.n;
+    if (V == 7) {
+        const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
+                                         m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
+        const float c[7] = {k.m, k.mom.x, k.mom.y, k.mom.z, k.J.x, k.J.y, k.J.z};
 #pragma unroll
-            for (int v = 0; v < V; ++v) e[v] = out[v];
-            e[7] = __int_as_float(cur);
-        }
-        int next = f > cur ? f : kMixed;
-        for (int d = 1; d < 8; d <<= 1) next = min(next, __shfl_xor_sync(gmask, next, d));
-        cur = next;
-    }
-    if (s == 0) B.mixed_run[node * 8 + a] = (at << 4) | k;
-}
-
-// Mixed-cell pass of p2g: 8 lanes per (listed cell, corner), so the 64
-// threads of a cell are two whole warps and every warp handles one cell.
-__global__ void __launch_bounds__(256) k_p2g_mixed_cells(bm_params P, bm_buffers B) {
-    const int64_t threads = 64 * (int64_t)B.flags[BM_FLAG_MIXED_CELLS];
-    const int N = P.n;
-    const unsigned gmask = 0xffu << (threadIdx.x & 24);
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < threads; t += (int64_t)gridDim.x * blockDim.x) {
-        const int j = (int)(t >> 6), a = (int)(t >> 3) & 7, s = (int)t & 7;
-        const int c = B.mixed_cells[j];
-        const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-        const bool present = s < count;
-        const int p = b + s;
-        float vals[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        int f = kMixed;
-        if (present) {
-            const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
-                                             m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
-            vals[0] = k.m;
-            vals[1] = k.mom.x;
-            vals[2] = k.mom.y;
-            vals[3] = k.mom.z;
-            vals[4] = k.J.x;
-            vals[5] = k.J.y;
-            vals[6] = k.J.z;
-            f = field_of(B.fidx[p], a);
-        }
-        emit_runs<7>(P, B, vals, a, f, cell_base_node(P, c), gmask, (j * 8 + a) * 8);
+        for (int v = 0; v < V; ++v) e[v] = c[v];
+    } else {
+        const bm_v3 r = v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a));
+        const float c[3] = {r.x, r.y, r.z};
+#pragma unroll
+        for (int v = 0; v < V; ++v) e[v] = c[v];
     }
 }
-
-// The tree sum of field f over the particles of cell c at corner a when its
-// run was not stored; false if no particle of c has field f there.
-__device__ __noinline__ bool p2g_recompute(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
-    const int N = P.n;
+// The tree sum ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)) of slot_value over the
+// slots of cell c (the cell pass's tree); false if no particle of c has
+// field f at corner a.
+template <int V>
+__device__ __forceinline__ bool mixed_corner(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
     const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-    float slot[8][7];
     bool any = false;
-    for (int s = 0; s < 8; ++s) {
-        for (int v = 0; v < 7; ++v) slot[s][v] = 0.0f;
-        if (s < count && field_of(B.fidx[b + s], a) == f) {
-            const int p = b + s;
-            const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
-                                             m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
-            slot[s][0] = k.m;
-            slot[s][1] = k.mom.x;
-            slot[s][2] = k.mom.y;
-            slot[s][3] = k.mom.z;
-            slot[s][4] = k.J.x;
-            slot[s][5] = k.J.y;
-            slot[s][6] = k.J.z;
-            any = true;
-        }
+    float half[2][V];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float e0[V], e1[V], pair[V];
+        slot_value<V>(P, B, b, count, 4 * h, a, f, e0, any);
+        slot_value<V>(P, B, b, count, 4 * h + 1, a, f, e1, any);
+#pragma unroll
+        for (int v = 0; v < V; ++v) pair[v] = e0[v] + e1[v];
+        slot_value<V>(P, B, b, count, 4 * h + 2, a, f, e0, any);
+        slot_value<V>(P, B, b, count, 4 * h + 3, a, f, e1, any);
+#pragma unroll
+        for (int v = 0; v < V; ++v) half[h][v] = pair[v] + (e0[v] + e1[v]);
     }
-    for (int v = 0; v < 7; ++v)
-        out[v] = ((slot[0][v] + slot[1][v]) + (slot[2][v] + slot[3][v])) + ((slot[4][v] + slot[5][v]) + (slot[6][v] + slot[7][v]));
-    return any;
-}
-__device__ __noinline__ bool remap_recompute(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
-    const int N = P.n;
-    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-    float slot[8][3];
-    bool any = false;
-    for (int s = 0; s < 8; ++s) {
-        slot[s][0] = slot[s][1] = slot[s][2] = 0.0f;
-        if (s < count && field_of(B.fidx[b + s], a) == f) {
-            const bm_v3 r = v3_mul(ld3(B.v, N, b + s), P.mass * stencil_w(B, B.stencil_id[b + s], a));
-            slot[s][0] = r.x;
-            slot[s][1] = r.y;
-            slot[s][2] = r.z;
-            any = true;
-        }
-    }
-    for (int v = 0; v < 3; ++v)
-        out[v] = ((slot[0][v] + slot[1][v]) + (slot[2][v] + slot[3][v])) + ((slot[4][v] + slot[5][v]) + (slot[6][v] + slot[7][v]));
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = half[0][v] + half[1][v];
     return any;
 }
 
-// Contribution of corner a of node n to field f (V sums): the uniform
-// partial, the mixed corner's run entry, or a recomputation; false if none.
+// Contribution of corner a of node n to field f (V sums): the cell pass's
+// partial at a uniform corner, the tree sum over the cell's particles of
+// field f at a mixed one; false if none.
 template <int V>
 __device__ __forceinline__ bool corner_value(const bm_params& P, const bm_buffers& B, int n, int a, int f, float* out) {
     const int NC = P.node_count, plane = 8 * NC;
@@ -399,27 +328,13 @@ __device__ __forceinline__ bool corner_value(const bm_params& P, const bm_buffer
         return true;
     }
     if (flag != kMixed) return false;
-    const int run = B.mixed_run[n * 8 + a];
-    if (run < 0) {
-        if (V == 7) return p2g_recompute(P, B, cell_at(P, n, a), a, f, out);
-        return remap_recompute(P, B, cell_at(P, n, a), a, f, out);
-    }
-    const int start = run >> 4, len = run & 15;
-    for (int k = 0; k < len; ++k) {
-        const float* e = B.mixed_part + 8 * (start + k);
-        if (__float_as_int(e[7]) == f) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) out[v] = e[v];
-            return true;
-        }
-    }
-    return false;
+    return mixed_corner<V>(P, B, cell_at(P, n, a), a, f, out);
 }
 
 // p2g node sums + couple_and_velocity (material.py:127-152, 252-284) for the
 // single-field nodes, one thread per active node (a single-field node has no
 // mixed corner: each corner is field 0 or has no cell).  Also clears the
-// topology flag consumed by registration and the mixed-run counter.
+// topology flag consumed by registration.
 __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int write_sums) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) B.flags[BM_FLAG_TOPOLOGY_DIRTY] = 0;
@@ -631,31 +546,6 @@ __global__ void __launch_bounds__(256) k_g2p(bm_params P, bm_buffers B, float ha
         part[0] = sum[0];
         part[plane] = sum[1];
         part[2 * plane] = sum[2];
-    }
-}
-
-// Mixed-cell pass of the re-scatter (new particle velocities), 8 lanes per
-// (listed cell, corner) like k_p2g_mixed_cells.
-__global__ void __launch_bounds__(256) k_remap_mixed_cells(bm_params P, bm_buffers B) {
-    const int64_t threads = 64 * (int64_t)B.flags[BM_FLAG_MIXED_CELLS];
-    const int N = P.n;
-    const unsigned gmask = 0xffu << (threadIdx.x & 24);
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < threads; t += (int64_t)gridDim.x * blockDim.x) {
-        const int j = (int)(t >> 6), a = (int)(t >> 3) & 7, s = (int)t & 7;
-        const int c = B.mixed_cells[j];
-        const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-        const bool present = s < count;
-        const int p = b + s;
-        float vals[3] = {0.0f, 0.0f, 0.0f};
-        int f = kMixed;
-        if (present) {
-            const bm_v3 r = v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a));
-            vals[0] = r.x;
-            vals[1] = r.y;
-            vals[2] = r.z;
-            f = field_of(B.fidx[p], a);
-        }
-        emit_runs<3>(P, B, vals, a, f, cell_base_node(P, c), gmask, (j * 8 + a) * 8);
     }
 }
 
@@ -1012,20 +902,27 @@ __device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x
     return __ballot_sync(0xffffffffu, near);
 }
 
-// update_F_plastic / update_F_maxwell (material.py:445-475, 592-618) fused
-// with this substep's side labelling (run after the tool update); thread 0
-// advances the substep counter of the friction-history ping-pong.
-__global__ void __launch_bounds__(256, 4) k_fupdate_assign(bm_params P, bm_buffers B, int do_update, int cut_index, int cutting, int advance_step) {
+// contact.assign (contact.py:996-1039) for every knife, after this substep's
+// tool update: the warp's knife-band cull, then each particle's band and digit
+// tests.  Reads x and v last in the substep, which leaves them in L2 for the
+// next substep's contact pass.
+__global__ void __launch_bounds__(256) k_assign(bm_params P, bm_buffers B, int cut_index, int cutting) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = p < P.n;
+    const int N = P.n;
+    // the whole warp takes part in the knife mask, so no lane leaves before it
+    const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero();
+    const unsigned knives = band_knives(P, B, xp, active);
+    if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, ld3(B.v, N, p), knives);
+}
+
+// update_F_plastic / update_F_maxwell (material.py:445-475, 592-618); thread
+// 0 advances the substep counter of the friction-history ping-pong.
+__global__ void __launch_bounds__(256, 4) k_fupdate(bm_params P, bm_buffers B, int do_update, int advance_step) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
     const bool active = p < P.n;
     const int N = P.n, S = P.fmax * P.node_count;
-    if (cutting) {
-        // the whole warp takes part in the knife mask, so no lane leaves before it
-        const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero();
-        const unsigned knives = band_knives(P, B, xp, active);
-        if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, ld3(B.v, N, p), knives);
-    }
     if (!active) return;
     if (do_update) {
         const int sid = B.stencil_id[p], base = B.base_node[p];
@@ -1160,7 +1057,6 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
     const bm_buffers& B = s->B;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
-    k_p2g_mixed_cells<<<8 * 152, kBlock, 0, st>>>(P, B);
     k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
     k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
     if (P.viscous) {
@@ -1179,7 +1075,6 @@ void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     k_g2p<<<grid_for(cells8), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
-    k_remap_mixed_cells<<<8 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
 void launch_remap(const bm_solver* s, cudaStream_t st) {
@@ -1188,10 +1083,12 @@ void launch_remap(const bm_solver* s, cudaStream_t st) {
     k_remap_multi<<<4 * 152, kBlock, 0, st>>>(P, s->B);
 }
 
-void launch_fupdate_assign(const bm_solver* s, int do_update, int cut_index, int cutting, int advance_step,
-                           cudaStream_t st) {
-    const bm_params& P = s->P;
-    k_fupdate_assign<<<grid_for(P.n), kBlock, 0, st>>>(P, s->B, do_update, cut_index, cutting, advance_step);
+void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st) {
+    if (do_update || advance_step) k_fupdate<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, do_update, advance_step);
+}
+
+void launch_assign(const bm_solver* s, int cut_index, int cutting, cudaStream_t st) {
+    if (cutting) k_assign<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, cut_index, cutting);
 }
 
 void launch_refresh_stress(const bm_solver* s, cudaStream_t st) {

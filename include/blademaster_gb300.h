@@ -64,7 +64,6 @@ typedef struct bm_params {
     int32_t pair_capacity;     /* friction-history hash table size (power of two) */
     int32_t bucket_mask;       /* pair search buckets - 1 (power of two) */
     int32_t candidate_capacity;
-    int32_t mixed_capacity;    /* entries of buffers.mixed_part */
     int32_t pad_sizes;
     /* mode flags */
     int32_t tool_model;        /* -1 external, 0 guided, 1 free/servo (solver.py:571-576) */
@@ -131,9 +130,6 @@ typedef struct bm_buffers {
     float* remap_v;      /* [3][fmax * node_count] coupled remapped momentum / mass */
     float* cell_part;    /* [7][8][node_count] cell-corner partial sums: from the cell whose corner a is node n */
     uint8_t* cell_field; /* [node_count][8] field index of a uniform cell corner, 255 mixed, 254 no cell */
-    int32_t* mixed_run;  /* [node_count][8] start << 4 | length of a mixed corner's per-field partials, -1 none */
-    float* mixed_part;   /* [mixed_capacity][8] per-field partials of mixed corners (7 sums, field as float):
-                          * 8 entries for each corner of each listed mixed cell, (listed index * 8 + corner) * 8 */
     int32_t* multi_nodes;/* [active_nodes] nodes with more than one field */
     int32_t* mixed_cells;/* [cells] cells whose particles map to different fields at some corner */
     /* pair contact */
@@ -356,8 +352,9 @@ int bm_embed_vertices(const bm_embedding* e, int vertex_count, const int64_t* ve
 #define BM_STAGE_G2P 5       /* g2p of g2p_remap */
 #define BM_STAGE_REMAP 6     /* remap scatter + couple */
 #define BM_STAGE_TOOL 7      /* tool.step / finish_external_step */
-#define BM_STAGE_FUPDATE 8   /* update_F + stress + assign */
-#define BM_STAGES 9
+#define BM_STAGE_FUPDATE 8   /* update_F + stress */
+#define BM_STAGE_ASSIGN 9    /* contact.assign (side labels) */
+#define BM_STAGES 10
 
 /* The batch of bm_substeps launched eagerly with a CUDA event pair around
  * every stage; stage_ms[BM_STAGES] receives the summed device time of each
