@@ -881,23 +881,35 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
     }
 }
 
-// Knives whose labelling band may hold some particle of this warp (the same
-// mask in every lane): a knife is left out when the warp's bounding box lies
-// beyond the per-particle band pre-test of assign_sides on the knife's x or
-// y axis, plus 1 um for rounding.
-__device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, bool active) {
+// Knives that may label some particle of this warp (the same mask in every
+// lane).  assign_sides labels a particle only inside the knife's band (within
+// 6 h on the knife's x axis and the half length on its y axis) and either
+// just behind the edge (local z in [0, back], back = 2 h + max(advance dt, 0)
+// with advance <= |edge velocity| + |v|) or pinched at the board (the edge
+// within one radius of z = 0 and the particle within one radius above it).
+// A knife is left out when the warp's bounding box, widened by 2 um for
+// rounding, misses the band or misses both the slab behind the edge and the
+// pinch region; every particle of the warp then fails assign_sides' tests.
+__device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x, float speed, bool active) {
     bm_v3 c, e;
-    float unused;
+    float vmax;
     bool any;
-    warp_box(x, 0.0f, active, &c, &e, &unused, &any);
+    warp_box(x, speed, active, &c, &e, &vmax, &any);
     if (!any) return 0u;
     const int k = threadIdx.x & 31;
     bool near = false;
     if (k < P.tool_count) {
         const ToolF T = load_tool(B.tool_f + BM_TOOL_F_WORDS * k);
         const bm_v3 d = v3_sub(c, T.edge);
-        near = !(fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) > 6.0f * P.spacing + 2.0e-6f ||
-                 fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + 2.0e-6f);
+        const float slack = 2.0e-6f;
+        const bool band = !(fabsf(v3_dot(d, T.ax)) - box_reach(T.ax, e) > 6.0f * P.spacing + slack ||
+                            fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + slack);
+        const float z = v3_dot(d, T.az), reach = box_reach(T.az, e);
+        const float back = 2.0f * P.spacing + P.dt * (v3_len(T.edge_vel) + vmax);
+        const bool behind = z + reach >= -slack && z - reach <= back + slack;
+        const float sway = P.half[1] * fabsf(T.ay.z);  // edge height change along the blade
+        const bool pinch = T.edge.z - sway <= P.radius + slack && c.z - e.z <= T.edge.z + sway + P.radius + slack;
+        near = band && (behind || pinch);
     }
     return __ballot_sync(0xffffffffu, near);
 }
@@ -911,9 +923,9 @@ __global__ void __launch_bounds__(256) k_assign(bm_params P, bm_buffers B, int c
     const bool active = p < P.n;
     const int N = P.n;
     // the whole warp takes part in the knife mask, so no lane leaves before it
-    const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero();
-    const unsigned knives = band_knives(P, B, xp, active);
-    if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, ld3(B.v, N, p), knives);
+    const bm_v3 xp = active ? ld3(B.x, N, p) : v3_zero(), vp = active ? ld3(B.v, N, p) : v3_zero();
+    const unsigned knives = band_knives(P, B, xp, v3_len(vp), active);
+    if (active && knives != 0u) assign_sides(P, B, p, cut_index, cutting, xp, vp, knives);
 }
 
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618); thread
