@@ -113,7 +113,6 @@ __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 // field by the same tree straight from the cell's particles.
 
 constexpr int kMixed = 255;
-constexpr int kAbsent = 254;
 constexpr unsigned kFull = 0xffffffffu;
 
 // Reduce-scatter over the 8 lanes of a cell group: vals[c][v] holds this
