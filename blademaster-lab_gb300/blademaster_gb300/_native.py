@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu", "bm_embed.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu", "bm_embed.cu", "bm_topocut.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -134,6 +134,10 @@ class Embedding(ctypes.Structure):
     _fields_ = _struct_fields("bm_embedding")
 
 
+class TopoCutGrid(ctypes.Structure):
+    _fields_ = _struct_fields("bm_topocut_grid")
+
+
 def header_constant(name):
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
     m = re.search(r"#define %s \(?([^\n]+)" % name, text)
@@ -201,6 +205,10 @@ def _declare(lib):
         "bm_components": ([vp, vp, vp, vp, vp, vp, vp], i),
         "bm_embed_nodes": ([vp, vp, vp, vp, vp, ctypes.c_int64, i, vp, vp, vp, vp], i),
         "bm_embed_vertices": ([vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
+        "bm_topocut_sdf": ([vp, vp, i, vp, vp, vp, vp, vp, vp, vp], i),
+        "bm_topocut_count": ([vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
+        "bm_topocut_emit": ([vp, vp, vp, vp, vp, vp, vp, vp], i),
+        "bm_topocut_cluster": ([vp, i, vp, vp, vp, i, ctypes.c_float, ctypes.c_float, vp, vp], i),
         "bm_count_embedded": ([vp, i, vp], i),
         "bm_validate_interval": ([vp, vp], i),
         "bm_read_accumulators": ([vp, vp, vp, vp, vp, vp], i),

@@ -343,6 +343,43 @@ int bm_embed_nodes(const bm_embedding* e, const void* x, const void* F, const in
 int bm_embed_vertices(const bm_embedding* e, int vertex_count, const int64_t* vertex_codes, const int32_t* corners,
                       const void* corner_weights, const void* x, const void* F, const int64_t* codes, void* vertices,
                       int32_t* counts, void* stream);
+/* TopoCut topology discovery for the MLS baseline (topocut_topology.py:31-229).
+ * Voxel points (i, j, k) sit at lower + voxel * (i, j, k), dims[] per axis,
+ * values stored row-major [dims0][dims1][dims2].  Particles are binned in
+ * cubes of edge `reach` (bin_dims[] of them from `lower`).  poses: [pose_count]
+ * knife poses of the carved trajectory, 7 floats each (position, quaternion
+ * xyzw), half: the knife half extents.  Device pointers throughout. */
+typedef struct bm_topocut_grid {
+    int32_t dims[3], bin_dims[3];
+    float lower[3], voxel, radius, reach, half[3];
+    int32_t pose_count;
+    const float* poses;
+} bm_topocut_grid;
+/* particle_sdf (topocut_topology.py:39-64): field = max(min |v - x_p| - radius,
+ * -v_z) over particles within reach, raised to one voxel inside any carved
+ * knife box.  x: [n][3].  Workspace: bin_start [bins + 1], bin_fill [bins],
+ * items [n], partials [bins / 1024 + 1], ticket [1] (zero). */
+int bm_topocut_sdf(const bm_topocut_grid* g, const float* x, int n, float* field, int32_t* bin_start,
+                   int32_t* bin_fill, int32_t* items, int32_t* partials, int32_t* ticket, void* stream);
+/* Zero isosurface of `field` (value < 0 inside) by marching tetrahedra, first
+ * pass: triangles per cube (cube_tris, tri_start = their exclusive scan,
+ * [cubes]) and crossed lattice edges (edge_used, edge_index = vertex index,
+ * [points * 7]); totals[0] triangles, totals[1] vertices.  partials holds
+ * points * 7 / 1024 + 1 ints. */
+int bm_topocut_count(const bm_topocut_grid* g, const float* field, int32_t* cube_tris, int32_t* tri_start,
+                     int32_t* edge_used, int32_t* edge_index, int32_t* partials, int32_t* ticket, int32_t* totals,
+                     void* stream);
+/* Second pass: vertices [totals[1]][3] and triangles [totals[0]][3], each
+ * oriented from the inside to the outside; vertices are shared along edges. */
+int bm_topocut_emit(const bm_topocut_grid* g, const float* field, const int32_t* tri_start, const int32_t* edge_used,
+                    const int32_t* edge_index, float* vertices, int32_t* triangles, void* stream);
+/* nearest_cluster (topocut_topology.py:67-78): labels[p] = the mesh (triangles
+ * mesh_start[m] .. mesh_start[m+1]) with the smallest signed distance to x_p
+ * below tau (negative inside by winding number; meshes farther than reach are
+ * skipped), else -1. */
+int bm_topocut_cluster(const float* x, int n, const float* vertices, const int32_t* triangles,
+                       const int32_t* mesh_start, int mesh_count, float tau, float reach, int32_t* labels,
+                       void* stream);
 /* Stages of one substep, in launch order (profiling). */
 #define BM_STAGE_PROLOGUE 0  /* clear_pair_slots + clear_step */
 #define BM_STAGE_RIGID 1     /* rigid_and_speed + extra_blade */
