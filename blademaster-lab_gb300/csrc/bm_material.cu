@@ -262,18 +262,16 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     }
 }
 
-// The V values at corner a of slot s of the cell whose particles are
-// [b, b + count): P2G sums (V = 7) or re-scatter momenta (V = 3) of a
-// particle with field f there, else +0.
+// The V values at corner a of slot s of the cell whose particles start at b:
+// P2G sums (V = 7) or re-scatter momenta (V = 3) when bit s of `match` says
+// that slot holds a particle with the wanted field there, else +0.
 template <int V>
-__device__ __forceinline__ void slot_value(const bm_params& P, const bm_buffers& B, int b, int count, int s, int a,
-                                           int f, float (&e)[V], bool& any) {
+__device__ __forceinline__ void slot_value(const bm_params& P, const bm_buffers& B, int b, unsigned match, int s, int a,
+                                           float (&e)[V]) {
 #pragma unroll
     for (int v = 0; v < V; ++v) e[v] = 0.0f;
-    if (s >= count) return;
+    if (((match >> s) & 1u) == 0u) return;
     const int p = b + s;
-    if (field_of(B.fidx[p], a) != f) return;
-    any = true;
     const int N = P.n;
     if (V == 7) {
         const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
@@ -290,27 +288,32 @@ __device__ __forceinline__ void slot_value(const bm_params& P, const bm_buffers&
 }
 // The tree sum ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)) of slot_value over the
 // slots of cell c (the cell pass's tree); false if no particle of c has
-// field f at corner a.
+// field f at corner a.  The slots' field words are read first, all at once,
+// so only the matching slots' data follow.
 template <int V>
 __device__ __forceinline__ bool mixed_corner(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
     const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
-    bool any = false;
+    unsigned match = 0u;
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+        if (s < count && field_of(B.fidx[b + s], a) == f) match |= 1u << s;
+    if (match == 0u) return false;
     float half[2][V];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         float e0[V], e1[V], pair[V];
-        slot_value<V>(P, B, b, count, 4 * h, a, f, e0, any);
-        slot_value<V>(P, B, b, count, 4 * h + 1, a, f, e1, any);
+        slot_value<V>(P, B, b, match, 4 * h, a, e0);
+        slot_value<V>(P, B, b, match, 4 * h + 1, a, e1);
 #pragma unroll
         for (int v = 0; v < V; ++v) pair[v] = e0[v] + e1[v];
-        slot_value<V>(P, B, b, count, 4 * h + 2, a, f, e0, any);
-        slot_value<V>(P, B, b, count, 4 * h + 3, a, f, e1, any);
+        slot_value<V>(P, B, b, match, 4 * h + 2, a, e0);
+        slot_value<V>(P, B, b, match, 4 * h + 3, a, e1);
 #pragma unroll
         for (int v = 0; v < V; ++v) half[h][v] = pair[v] + (e0[v] + e1[v]);
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) out[v] = half[0][v] + half[1][v];
-    return any;
+    return true;
 }
 
 // Contribution of corner a of node n to field f (V sums): the cell pass's
