@@ -100,21 +100,27 @@ __device__ __forceinline__ float order_value(int k) { return __int_as_float(k ^ 
 // lanes and the largest of their `speed` values.  All 32 lanes must call;
 // `*any` is false when no lane is active.  The box is widened by 1 um so that
 // it still contains every position after the rounding of centre and extent.
-// Minima and maxima are exact (integer warp reductions of order keys).
+// Minima and maxima are exact (float warp reductions); a NaN among the active
+// values makes the result NaN, which every knife test keeps.
+__device__ __forceinline__ float warp_min(float v) {
+    float r;
+    asm("redux.sync.min.NaN.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    float r;
+    asm("redux.sync.max.NaN.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
+}
 __device__ __forceinline__ void warp_box(bm_v3 x, float speed, bool active, bm_v3* centre, bm_v3* extent,
                                          float* max_speed, bool* any) {
-    const unsigned all = 0xffffffffu;
-    *any = __any_sync(all, active);
-    const int big = 0x7fffffff, small = (int)0x80000000;
-    const bm_v3 lo = v3(order_value(__reduce_min_sync(all, active ? order_key(x.x) : big)),
-                        order_value(__reduce_min_sync(all, active ? order_key(x.y) : big)),
-                        order_value(__reduce_min_sync(all, active ? order_key(x.z) : big)));
-    const bm_v3 hi = v3(order_value(__reduce_max_sync(all, active ? order_key(x.x) : small)),
-                        order_value(__reduce_max_sync(all, active ? order_key(x.y) : small)),
-                        order_value(__reduce_max_sync(all, active ? order_key(x.z) : small)));
+    *any = __any_sync(0xffffffffu, active);
+    const float inf = __int_as_float(0x7f800000);
+    const bm_v3 lo = v3(warp_min(active ? x.x : inf), warp_min(active ? x.y : inf), warp_min(active ? x.z : inf));
+    const bm_v3 hi = v3(warp_max(active ? x.x : -inf), warp_max(active ? x.y : -inf), warp_max(active ? x.z : -inf));
     *centre = v3_mul(v3_add(lo, hi), 0.5f);
     *extent = v3_add(v3_mul(v3_sub(hi, lo), 0.5f), v3(1.0e-6f, 1.0e-6f, 1.0e-6f));
-    *max_speed = order_value(__reduce_max_sync(all, active ? order_key(speed) : small));
+    *max_speed = warp_max(active ? speed : -inf);
 }
 
 // Projection radius of a box with half extent e on direction a.

@@ -908,9 +908,10 @@ __device__ unsigned band_knives(const bm_params& P, const bm_buffers& B, bm_v3 x
                             fabsf(v3_dot(d, T.ay)) - box_reach(T.ay, e) > P.half[1] + slack);
         const float z = v3_dot(d, T.az), reach = box_reach(T.az, e);
         const float back = 2.0f * P.spacing + P.dt * (v3_len(T.edge_vel) + vmax);
-        const bool behind = z + reach >= -slack && z - reach <= back + slack;
+        // written as "not certainly outside", so a NaN in the box keeps the knife
+        const bool behind = !(z + reach < -slack || z - reach > back + slack);
         const float sway = P.half[1] * fabsf(T.ay.z);  // edge height change along the blade
-        const bool pinch = T.edge.z - sway <= P.radius + slack && c.z - e.z <= T.edge.z + sway + P.radius + slack;
+        const bool pinch = !(T.edge.z - sway > P.radius + slack || c.z - e.z > T.edge.z + sway + P.radius + slack);
         near = band && (behind || pinch);
     }
     return __ballot_sync(0xffffffffu, near);
