@@ -186,9 +186,13 @@ def run_sweep(args, rank, world):
     from blademaster_gb300.solver import Solver
     from blademaster_gb300.sweep import instances
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from blademaster_gb300 import replicas
+
+    dist, rank, world, local = replicas.init()
     torch.cuda.set_device(local)
-    sweep = instances(args.instances, seed=rank)
+    # weak scaling: each rank takes its share of one list of instances per rank
+    everything = instances(args.instances * world, seed=0)
+    sweep = [everything[i] for i in replicas.shard(len(everything), rank, world)]
     solvers = [Solver(i.config, device=f"cuda:{local}") for i in sweep]
     batch = SolverBatch(solvers)
     steps = [int(round(0.001 / s.config.dt)) for s in solvers]
@@ -208,11 +212,13 @@ def run_sweep(args, rank, world):
     tuner.tune(batch, lambda i: states(), 0.001, strict=False)
     for _ in range(args.warmup):
         batch.advance(states(), 0.001, strict=False)
-    torch.cuda.synchronize()
+    replicas.barrier(dist, torch.cuda.current_device())
     begin = time.perf_counter()
     for _ in range(args.steps):
         batch.advance(states(), 0.001, strict=False)
-    batched = (time.perf_counter() - begin) / args.steps
+    replicas.barrier(dist, torch.cuda.current_device())
+    batched = replicas.max_over_ranks(dist, (time.perf_counter() - begin) / args.steps)
+    work = replicas.sum_over_ranks(dist, work)
     ports = [ExternalToolPort(s) for s in solvers]
 
     def port_interval(port, state):
@@ -224,26 +230,32 @@ def run_sweep(args, rank, world):
     for p, i in zip(ports, sweep):  # warm the per-instance graphs
         port_interval(p, i.state(k, start_gap=-0.001))
     k += 1
-    torch.cuda.synchronize()
+    replicas.barrier(dist, torch.cuda.current_device())
     begin = time.perf_counter()
     for _ in range(max(1, args.steps // 4)):
         for p, s_ in zip(ports, states()):
             port_interval(p, s_)
-    single = (time.perf_counter() - begin) / max(1, args.steps // 4)
+    replicas.barrier(dist, torch.cuda.current_device())
+    single = replicas.max_over_ranks(dist, (time.perf_counter() - begin) / max(1, args.steps // 4))
+    failures = replicas.sum_over_ranks(dist, len(batch.failures))
+    particles = replicas.sum_over_ranks(dist, sum(s.n for s in solvers))
     if rank == 0:
         print(json.dumps({
-            "metric": METRIC, "value": world * work / batched, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": work / batched, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": batched * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"sweep_{args.instances}_hcylinders", "instances": args.instances,
-                       "particles": sum(s.n for s in solvers), "substeps_per_interval": steps[0],
+                       "particles": int(particles), "substeps_per_interval": steps[0],
                        "lanes": batch.lanes, "tuned": getattr(tuner, "timings", {}),
                        "step": "one 1 ms coupling interval of every instance, host knife states in, reactions out"},
-            "per_instance": {"value": world * work / single, "ms_per_step": single * 1e3,
+            "per_instance": {"value": work / single, "ms_per_step": single * 1e3,
                              "mode": "one ExternalToolPort.advance (graph) per instance per interval"},
             "batched_speedup": single / batched,
-            "failed_instance_intervals": len(batch.failures),
+            "failed_instance_intervals": int(failures),
+            "parallelism": f"replicas x{world}, {args.instances} instances per rank",
         }), flush=True)
+    if dist:
+        dist.destroy_process_group()
 
 
 def run_reference(args, rank, world):
@@ -301,12 +313,10 @@ def main():
 
     import torch
 
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    from blademaster_gb300 import replicas
 
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dist, rank, world, local = replicas.init()
+    torch.cuda.set_device(local)
 
     from blademaster_gb300 import _native
     from blademaster_gb300.solver import Solver
@@ -341,26 +351,18 @@ def main():
     clock_file = tempfile.NamedTemporaryFile(suffix=".csv", delete=False).name
     sampler = sample_clocks(clock_file)
     time.sleep(0.5)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
+    replicas.barrier(dist, torch.cuda.current_device())
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     counters_before = s._t["flags"].cpu().numpy().copy()
     start.record()
     run(args.steps)
     end.record()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist, torch.cuda.current_device())
     if sampler:
         time.sleep(0.3)
         sampler.terminate()
         sampler.wait()
-    ms = start.elapsed_time(end)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(dist, start.elapsed_time(end), torch.cuda.current_device())
     slots = int(s._t["nfield"].sum().item())
     counters_after = s._t["flags"].cpu().numpy()
     def delta(name):
@@ -410,7 +412,7 @@ def main():
         s.step_count += 1
         pinned_state.copy_(s._t["tool"], non_blocking=True)
         torch.cuda.current_stream().synchronize()
-    e2e_s = time.perf_counter() - begin
+    e2e_s = replicas.max_over_ranks(dist, time.perf_counter() - begin, torch.cuda.current_device())
     e2e_value = world * s.n * args.e2e_steps / e2e_s
 
     errors = s.errors.numpy().tolist()
