@@ -83,6 +83,23 @@ def test_guided_cut_substeps_are_bitexact(yield_stress):
     assert np.count_nonzero(g.codes.numpy()) > 0
 
 
+def test_ragged_particle_count_cut_is_bitexact():
+    # 2640 particles (jittered): neither a multiple of 32 nor of 256, so every
+    # kernel's last warp and block run partly empty
+    cfg = Config(size=(0.05, 0.03, 0.02), grid_spacing=0.0045, sampling_seed=3, yield_stress=1500.0,
+                 blade_half_size=(0.0005, 0.02, 0.02))
+    g, c = both(cfg)
+    assert g.n % 32 != 0
+    g.tool_pos.assign([[0.001, 0.0, 0.039]])
+    c.set("tool_pos", [[0.001, 0.0, 0.039]])
+    for _ in range(60):
+        g.step((0.001, 0.0, 0.004), cutting=True)
+        c.step((0.001, 0.0, 0.004), cutting=True)
+    assert_same(g, c, EXACT + ("Fp",))
+    np.testing.assert_array_equal(g.reaction.numpy(), c.get("reaction").astype(np.float32))
+    assert np.count_nonzero(g.codes.numpy()) > 0
+
+
 def test_graph_replay_is_bitexact_with_eager_and_oracle():
     cfg = replace(Config(), free_blade=True)
     eager, graphed = Solver(cfg), Solver(cfg)
