@@ -127,9 +127,11 @@ class SolverBatch:
             host[i, 7:10], host[i, 10:13] = state.linear_velocity, state.angular_velocity
             host[i, 13:] = state.mobility.ravel()
         self._packed.copy_(self._host_packed, non_blocking=True)
+        for s in self.solvers:
+            s._sync_step()
         _native.check(self._lib.bm_graph_launch(self.graph(steps, cutting, cut, lanes), self._stream))
         for s, n in zip(self.solvers, steps):
-            s.step_count += n
+            s._advanced(n)
         readback = time.perf_counter()
         self.timing_s["submission"] += readback - begin
         interval = self._interval.cpu().numpy()

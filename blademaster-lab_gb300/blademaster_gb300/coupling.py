@@ -111,7 +111,7 @@ class ExternalToolPort:
             [state.position, state.orientation_xyzw, state.linear_velocity, state.angular_velocity, state.mobility.ravel()]
         ).astype(np.float32)
         s._t["packed"].copy_(torch.as_tensor(packed, device=s.device))
-        s._flag("STEP", s.step_count)
+        s._sync_step()
         extra = dict(external_load=1, external_finish=1, record_samples=samples, hold_pose=int(held_pose))
         if graph:
             handle = s.prepare(np.zeros((steps, 3), np.float32), cutting, cut_index, tag=("external",), use_targets=0, **extra)
@@ -119,7 +119,7 @@ class ExternalToolPort:
         else:
             args = s._step_args(steps, cutting, cut_index, use_targets=0, **extra)
             _native.check(s._lib.bm_substeps(s._handle, ctypes.byref(args), s._stream))
-        s.step_count += steps
+        s._advanced(steps)
         readback_begin = time.perf_counter()
         self.timing_s["submission"] += readback_begin - submission_begin
         out = s._t["result"][: 10 + 7 * samples].cpu().numpy().astype(np.float64)

@@ -337,6 +337,7 @@ class Solver:
         self.blade_constraint = BladeConstraint(self) if hold else None
         self.field_codes = self.codes
         self.step_count = 0
+        self._device_step = 0  # the substep counter the device holds (flags start at zero)
         self.cut_index = 0
         self._batches = {}
         self.graph_build_s = 0.0
@@ -471,6 +472,20 @@ class Solver:
 
     def _call(self, fn, *args):
         _native.check(getattr(self._lib, fn)(self._handle, *args))
+
+    def _sync_step(self):
+        """Make the device's substep counter (friction-history parity) equal step_count.
+
+        Every substep launch advances the device counter and step_count
+        together, so this writes only when something else moved one of them.
+        """
+        if self._device_step != self.step_count:
+            self._flag("STEP", self.step_count)
+            self._device_step = self.step_count
+
+    def _advanced(self, substeps):
+        self.step_count += substeps
+        self._device_step += substeps
 
     def _flag(self, name, value=None):
         idx = _native.FLAG[name]
@@ -690,7 +705,7 @@ class Solver:
 
     def particle_contacts(self):
         """Contacts between particles on incompatible sides of a cut, with friction history."""
-        self._flag("STEP", self.step_count)
+        self._sync_step()
         self._call("bm_particle_contacts", self._stream)
 
     def assign_sides(self, cut_index, cutting=True):
@@ -761,11 +776,11 @@ class Solver:
 
     def _step_kernels(self, target_edge, cutting, cut_index, buffer=None, index=0, rotations=None, orientation=None):
         """One substep: contacts, material update, tool update, side labels."""
-        self._flag("STEP", self.step_count)
+        self._sync_step()
         self._write_targets([target_edge], [orientation if orientation is not None else [0.0, 0.0, 0.0, 1.0]])
         args = self._step_args(1, cutting, cut_index, use_targets=0)
         _native.check(self._lib.bm_substeps(self._handle, ctypes.byref(args), self._stream))
-        self.step_count += 1
+        self._advanced(1)
 
     def advance(self, targets, cutting=True, cut_index=0, graph=True, orientations=None):
         """Submit exact per-substep targets, including every intermediate contact (solver.py:942-973)."""
@@ -788,11 +803,11 @@ class Solver:
             return
         for start in range(0, len(targets), MAX_BATCH):
             chunk = slice(start, start + MAX_BATCH)
-            self._flag("STEP", self.step_count)
+            self._sync_step()
             graph_handle = self.prepare(targets[chunk], cutting, cut_index, orientations[chunk])
             self._write_targets(targets[chunk], orientations[chunk])
             _native.check(self._lib.bm_graph_launch(graph_handle, self._stream))
-            self.step_count += len(targets[chunk])
+            self._advanced(len(targets[chunk]))
 
     def prepare(self, targets, cutting=True, cut_index=0, orientations=None, tag=None, **extra):
         """Capture one batch of substeps as a CUDA graph, cached by its shape (solver.py:975-1019)."""
