@@ -12,8 +12,8 @@ struct bm_solver {
     float* viscous_scratch;  // [9][n] inside B.scratch
     int32_t* scan_partials;  // inside B.scratch
     int64_t buckets;
-    cudaStream_t side;       // knife integration runs here, concurrent with the transfers
-    cudaEvent_t fork, join;
+    cudaStream_t side;       // registration and knife integration run here, beside the main chain
+    cudaEvent_t fork, join, register_fork, register_join;
 };
 
 struct bm_graph {
