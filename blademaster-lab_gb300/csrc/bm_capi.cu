@@ -122,12 +122,12 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         if (overlap) cudaStreamWaitEvent(st, s->register_join, 0);
         else bm::launch_register(s, field_codes, force_topology ? 1 : 0, st, 0);
         t.mark(4, st);
-        bm::launch_material(s, 0, st);
+        bm::launch_material(s, 0, st, overlap ? s->aux : nullptr);
         if (P.external_tool && !P.predict) bm::launch_hold(s, st);
         t.mark(5, st);
         bm::launch_g2p(s, st);
         t.mark(6, st);
-        bm::launch_remap(s, st);
+        bm::launch_remap(s, st, overlap ? s->aux : nullptr);
         t.mark(7, st);
         if (fork) cudaStreamWaitEvent(st, s->join, 0);
         else bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
@@ -214,17 +214,21 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     s->B = *buffers;
     s->buckets = (int64_t)P.bucket_mask + 1;
     layout_scratch(s);
-    s->side = nullptr;
-    s->fork = s->join = s->register_fork = s->register_join = nullptr;
+    s->side = s->aux = nullptr;
+    s->fork = s->join = s->register_fork = s->register_join = s->aux_fork = s->aux_join = nullptr;
     if (cudaMemset(s->B.scratch + 1, 0, 63 * sizeof(int32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->aux_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->aux_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->register_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->register_join, cudaEventDisableTiming) != cudaSuccess) {
         const int rc = check_cuda("solver streams");
-        if (s->side) cudaStreamDestroy(s->side);
-        for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join})
+        for (cudaStream_t q : {s->side, s->aux})
+            if (q) cudaStreamDestroy(q);
+        for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join})
             if (e) cudaEventDestroy(e);
         delete s;
         return rc;
@@ -235,12 +239,12 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
 
 int bm_solver_destroy(bm_solver* s) {
     if (!s) return BM_OK;
-    cudaStreamSynchronize(s->side);
-    cudaStreamDestroy(s->side);
-    cudaEventDestroy(s->fork);
-    cudaEventDestroy(s->join);
-    cudaEventDestroy(s->register_fork);
-    cudaEventDestroy(s->register_join);
+    for (cudaStream_t q : {s->side, s->aux}) {
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+    }
+    for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join})
+        cudaEventDestroy(e);
     delete s;
     return BM_OK;
 }

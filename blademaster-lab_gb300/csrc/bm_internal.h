@@ -13,7 +13,8 @@ struct bm_solver {
     int32_t* scan_partials;  // inside B.scratch
     int64_t buckets;
     cudaStream_t side;       // registration and knife integration run here, beside the main chain
-    cudaEvent_t fork, join, register_fork, register_join;
+    cudaStream_t aux;        // the multi-field node passes run here, beside the single-field ones
+    cudaEvent_t fork, join, register_fork, register_join, aux_fork, aux_join;
 };
 
 struct bm_graph {
@@ -26,9 +27,11 @@ namespace bm {
 // material
 // begin == 0: k_prologue of the same substep already began the registration.
 void launch_register(const bm_solver* s, const int64_t* field_codes, int force, cudaStream_t st, int begin = 1);
-void launch_material(const bm_solver* s, int write_sums, cudaStream_t st);
+// aux != nullptr: the multi-field node pass runs on aux beside the single-field
+// one (the two write disjoint slots), joined back into st.
+void launch_material(const bm_solver* s, int write_sums, cudaStream_t st, cudaStream_t aux = nullptr);
 void launch_g2p(const bm_solver* s, cudaStream_t st);
-void launch_remap(const bm_solver* s, cudaStream_t st);
+void launch_remap(const bm_solver* s, cudaStream_t st, cudaStream_t aux = nullptr);
 // update_F + stress (do_update) and the substep counter (advance_step).
 void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st);
 // contact.assign for every knife (nothing when cutting == 0).

@@ -113,6 +113,7 @@ __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
 // field by the same tree straight from the cell's particles.
 
 constexpr int kMixed = 255;
+constexpr int kAbsentCorner = 254;
 constexpr unsigned kFull = 0xffffffffu;
 
 // Reduce-scatter over the 8 lanes of a cell group: vals[c][v] holds this
@@ -262,75 +263,119 @@ __global__ void __launch_bounds__(256) k_p2g_cells(bm_params P, bm_buffers B) {
     }
 }
 
-// The V values at corner a of slot s of the cell whose particles start at b:
-// P2G sums (V = 7) or re-scatter momenta (V = 3) when bit s of `match` says
-// that slot holds a particle with the wanted field there, else +0.
+// A multi-field node staged in shared memory by its warp.  val[a][8 s + v]
+// holds the V values that slot s of the cell at corner a gives the node: the
+// contribution of that slot's particle at a mixed corner, the cell pass's
+// partial (in slot 0) at a uniform one.  field[a][s] is the field those
+// values belong to (-1: none) and flag[a] the corner's cell_field flag.  The
+// row pad puts the eight corners on different banks.
+struct NodeStage {
+    float val[8][8 * 8 + 1];
+    int field[8][9];
+    int flag[8];
+};
+
+// Stage 1, lane (g, s) = (lane / 8, lane % 8): slot s of corners 7 - g and
+// 3 - g.  Every load is issued without a branch (particle 0 stands in where
+// a slot is not needed), so the cell words, the particles and the stencil
+// rows of all 64 (corner, slot) pairs take three dependent round trips.
 template <int V>
-__device__ __forceinline__ void slot_value(const bm_params& P, const bm_buffers& B, int b, unsigned match, int s, int a,
-                                           float (&e)[V]) {
+__device__ __forceinline__ void stage_node(const bm_params& P, const bm_buffers& B, int n, NodeStage& st) {
+    const int lane = threadIdx.x & 31, g = lane >> 3, s = lane & 7;
+    const int N = P.n, NC = P.node_count, plane = 8 * NC;
 #pragma unroll
-    for (int v = 0; v < V; ++v) e[v] = 0.0f;
-    if (((match >> s) & 1u) == 0u) return;
-    const int p = b + s;
-    const int N = P.n;
-    if (V == 7) {
-        const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
-                                         m33_scale(ld9(B.stress, N, p), P.dt * P.volume), B.stencil_id[p], a);
-        const float c[7] = {k.m, k.mom.x, k.mom.y, k.mom.z, k.J.x, k.J.y, k.J.z};
+    for (int h = 0; h < 2; ++h) {
+        const int a = 7 - (4 * h + g);
+        const int c = cell_at(P, n, a);
+        const int flag = B.cell_field[n * 8 + a];
+        int b = 0, count = 0;
+        if (c >= 0) {
+            b = B.cell_start[c];
+            count = B.cell_start[c + 1] - b;
+        }
+        const bool mixed = flag == kMixed && s < count;
+        const bool uniform = flag != kMixed && flag != kAbsentCorner && s == 0;
+        const int p = mixed ? b + s : 0;
+        const uint64_t fidx = B.fidx[p];
+        const int sid = B.stencil_id[p];
+        float e[V];
+        if (V == 7) {
+            const P2GContrib k = p2g_contrib(P, B, ld3(B.v, N, p), ld3(B.impulses, N, p),
+                                             m33_scale(ld9(B.stress, N, p), P.dt * P.volume), sid, a);
+            const float c7[7] = {k.m, k.mom.x, k.mom.y, k.mom.z, k.J.x, k.J.y, k.J.z};
 #pragma unroll
-        for (int v = 0; v < V; ++v) e[v] = c[v];
-    } else {
-        const bm_v3 r = v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, B.stencil_id[p], a));
-        const float c[3] = {r.x, r.y, r.z};
+            for (int v = 0; v < V; ++v) e[v] = c7[v];
+        } else {
+            const bm_v3 r = v3_mul(ld3(B.v, N, p), P.mass * stencil_w(B, sid, a));
+            const float c3[3] = {r.x, r.y, r.z};
 #pragma unroll
-        for (int v = 0; v < V; ++v) e[v] = c[v];
+            for (int v = 0; v < V; ++v) e[v] = c3[v];
+        }
+        const float* part = B.cell_part + a * NC + n;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float u = part[v * plane];
+            st.val[a][8 * s + v] = mixed ? e[v] : (uniform ? u : 0.0f);
+        }
+        st.field[a][s] = mixed ? field_of(fidx, a) : (uniform ? flag : -1);
+        if (s == 0) st.flag[a] = flag;
     }
 }
-// The tree sum ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)) of slot_value over the
-// slots of cell c (the cell pass's tree); false if no particle of c has
-// field f at corner a.  The slots' field words are read first, all at once,
-// so only the matching slots' data follow.
+
+// Stage 2: the values corner a gives field f - the tree sum
+// ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)) over the slots of field f at a mixed
+// corner (+0 for the others, the cell pass's tree), the cell partial at a
+// uniform corner of field f; false if the corner gives f nothing.
 template <int V>
-__device__ __forceinline__ bool mixed_corner(const bm_params& P, const bm_buffers& B, int c, int a, int f, float* out) {
-    const int b = B.cell_start[c], count = B.cell_start[c + 1] - b;
+__device__ __forceinline__ bool staged_corner(const NodeStage& st, int a, int f, float (&out)[V]) {
+    const int flag = st.flag[a];
+    if (flag != kMixed) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = st.val[a][v];
+        return flag == f;
+    }
     unsigned match = 0u;
 #pragma unroll
     for (int s = 0; s < 8; ++s)
-        if (s < count && field_of(B.fidx[b + s], a) == f) match |= 1u << s;
-    if (match == 0u) return false;
+        if (st.field[a][s] == f) match |= 1u << s;
     float half[2][V];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        float e0[V], e1[V], pair[V];
-        slot_value<V>(P, B, b, match, 4 * h, a, e0);
-        slot_value<V>(P, B, b, match, 4 * h + 1, a, e1);
+        float e[4][V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) pair[v] = e0[v] + e1[v];
-        slot_value<V>(P, B, b, match, 4 * h + 2, a, e0);
-        slot_value<V>(P, B, b, match, 4 * h + 3, a, e1);
+        for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int v = 0; v < V; ++v) half[h][v] = pair[v] + (e0[v] + e1[v]);
+            for (int v = 0; v < V; ++v) e[k][v] = ((match >> (4 * h + k)) & 1u) ? st.val[a][8 * (4 * h + k) + v] : 0.0f;
+#pragma unroll
+        for (int v = 0; v < V; ++v) half[h][v] = (e[0][v] + e[1][v]) + (e[2][v] + e[3][v]);
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) out[v] = half[0][v] + half[1][v];
-    return true;
+    return match != 0u;
 }
 
-// Contribution of corner a of node n to field f (V sums): the cell pass's
-// partial at a uniform corner, the tree sum over the cell's particles of
-// field f at a mixed one; false if none.
+// Stages 2 and 3 for fields f0 .. f0 + 3: lane (a, k) = (lane / 4, lane % 4)
+// forms corner a's values for field f0 + k; then every lane adds, for its
+// field f0 + lane % 4, the corners that have that field in ascending cell
+// index (a = 7 .. 0).
 template <int V>
-__device__ __forceinline__ bool corner_value(const bm_params& P, const bm_buffers& B, int n, int a, int f, float* out) {
-    const int NC = P.node_count, plane = 8 * NC;
-    const int flag = B.cell_field[n * 8 + a];
-    if (flag == f) {
-        const float* part = B.cell_part + a * NC + n;
+__device__ __forceinline__ void staged_sums(const NodeStage& st, int nf, int f0, float (&sum)[V]) {
+    const int lane = threadIdx.x & 31, k = lane & 3, f = f0 + k;
+    float cv[V];
+    const bool have = f < nf && staged_corner<V>(st, lane >> 2, f, cv);
+    const unsigned haves = __ballot_sync(kFull, have);
 #pragma unroll
-        for (int v = 0; v < V; ++v) out[v] = part[v * plane];
-        return true;
+    for (int v = 0; v < V; ++v) sum[v] = 0.0f;
+#pragma unroll
+    for (int a = 7; a >= 0; --a) {
+        const int src = 4 * a + k;
+        const bool use = (haves >> src) & 1u;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float x = __shfl_sync(kFull, cv[v], src);
+            if (use) sum[v] = sum[v] + x;
+        }
     }
-    if (flag != kMixed) return false;
-    return mixed_corner<V>(P, B, cell_at(P, n, a), a, f, out);
 }
 
 // p2g node sums + couple_and_velocity (material.py:127-152, 252-284) for the
@@ -375,63 +420,52 @@ __global__ void __launch_bounds__(256) k_p2g_grid(bm_params P, bm_buffers B, int
     st3(B.new_v, S, n, v3_div(v3_add(pm, jm), m));
 }
 
-// Multi-field nodes, one warp per listed node: lane (field f, corner a)
-// fetches one corner value, then the lane of corner 0 of each field adds the
-// eight in ascending cell index (a = 7 .. 0); fields are taken four at a time.
-// Then lane f evaluates the exchange of field f (couple_and_velocity_at).
+// Multi-field nodes, one warp per listed node: the node is staged (stage 1),
+// then fields are summed four at a time (stages 2 and 3).  With at most four
+// fields, lanes 0 .. 3 then hold every field's sums and evaluate the exchange
+// (couple_and_velocity_at) by shuffles; otherwise the sums go to memory and
+// lane f evaluates field f's exchange from there.
 __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B, int write_sums) {
+    __shared__ NodeStage stage[kBlock / 32];
+    NodeStage& st = stage[threadIdx.x >> 5];
     const int count = B.flags[BM_FLAG_MULTI];
-    const int S = P.fmax * P.node_count;
-    const int lane = threadIdx.x & 31;
+    const int NC = P.node_count, S = P.fmax * NC;
+    const int lane = threadIdx.x & 31, k = lane & 3;
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < count; w += warps) {
         const int n = B.multi_nodes[w];
         const int nf = B.nfield[n];
-        // sums: grid_mass, momentum (3), grid_impulse (3) through one store layout
-        const int lanef = lane >> 3, a = lane & 7;
+        const int slot = k * NC + n;
+        uint64_t oa = 0u, ta = 0u;
+        if (nf <= 4 && k < nf) {
+            oa = B.fones[slot];
+            ta = B.ftwos[slot];
+        }
+        stage_node<7>(P, B, n, st);
+        __syncwarp();
         for (int f0 = 0; f0 < nf; f0 += 4) {
-            const int f = f0 + lanef;
-            float val[7];
-            bool have = false;
-            if (f < nf) have = corner_value<7>(P, B, n, a, f, val);
-            if (!have)
-                for (int v = 0; v < 7; ++v) val[v] = 0.0f;
-            const unsigned haves = __ballot_sync(kFull, have);
-            float sum[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-            for (int c = 7; c >= 0; --c) {
-                const int src = (lane & 24) + c;
-                const bool use = (haves >> src) & 1u;
-                for (int v = 0; v < 7; ++v) {
-                    const float x = __shfl_sync(kFull, val[v], src);
-                    if (use) sum[v] = sum[v] + x;
-                }
-            }
+            float sum[7];
+            staged_sums<7>(st, nf, f0, sum);
+            const int f = f0 + k;
             if (nf <= 4) {
-                // every field's sums are in this warp (lane group g holds field g): exchange by
-                // shuffles in ascending field order, as the general path below does from memory
-                const int slot = f * P.node_count + n;
+                // every field's sums are in lanes 0 .. nf-1: exchange in ascending field
+                // order by shuffles, as the general path below does from memory
                 const float ma = sum[0];
                 const bm_v3 pa = v3(sum[1], sum[2], sum[3]), ja = v3(sum[4], sum[5], sum[6]);
-                uint64_t oa = 0u, ta = 0u;
-                if (f < nf) {
-                    oa = B.fones[slot];
-                    ta = B.ftwos[slot];
-                }
                 float total = 0.0f;
                 bm_v3 dm = v3_zero(), di = v3_zero();
                 for (int g = 0; g < nf; ++g) {
-                    const int src = 8 * g;
-                    const float mb = __shfl_sync(kFull, ma, src);
-                    const bm_v3 pb = v3(__shfl_sync(kFull, pa.x, src), __shfl_sync(kFull, pa.y, src), __shfl_sync(kFull, pa.z, src));
-                    const bm_v3 jb = v3(__shfl_sync(kFull, ja.x, src), __shfl_sync(kFull, ja.y, src), __shfl_sync(kFull, ja.z, src));
-                    const uint64_t ob = __shfl_sync(kFull, oa, src), tb = __shfl_sync(kFull, ta, src);
+                    const float mb = __shfl_sync(kFull, ma, g);
+                    const bm_v3 pb = v3(__shfl_sync(kFull, pa.x, g), __shfl_sync(kFull, pa.y, g), __shfl_sync(kFull, pa.z, g));
+                    const bm_v3 jb = v3(__shfl_sync(kFull, ja.x, g), __shfl_sync(kFull, ja.y, g), __shfl_sync(kFull, ja.z, g));
+                    const uint64_t ob = __shfl_sync(kFull, oa, g), tb = __shfl_sync(kFull, ta, g);
                     total = total + mb;
                     if (g != f && compatible_masks(oa, ta, ob, tb)) {
                         dm = v3_add(dm, v3_sub(v3_mul(pb, ma), v3_mul(pa, mb)));
                         di = v3_add(di, v3_sub(v3_mul(jb, ma), v3_mul(ja, mb)));
                     }
                 }
-                if (a == 0 && f < nf) {
+                if (lane < nf) {
                     B.grid_mass[slot] = ma;
                     if (write_sums) {
                         st3(B.momentum, S, slot, pa);
@@ -449,18 +483,18 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B, in
                 }
                 continue;
             }
-            if (a == 0 && f < nf) {
-                const int slot = f * P.node_count + n;
-                B.grid_mass[slot] = sum[0];
-                st3(B.momentum, S, slot, v3(sum[1], sum[2], sum[3]));
-                st3(B.grid_impulse, S, slot, v3(sum[4], sum[5], sum[6]));
+            if (lane < 4 && f < nf) {
+                const int sf = f * NC + n;
+                B.grid_mass[sf] = sum[0];
+                st3(B.momentum, S, sf, v3(sum[1], sum[2], sum[3]));
+                st3(B.grid_impulse, S, sf, v3(sum[4], sum[5], sum[6]));
             }
         }
+        __syncwarp();  // the stage is rewritten for the next node; the sums are visible to the warp
         if (nf <= 4) continue;
-        __syncwarp();
         // exchange (couple_and_velocity_at): lane f handles field f
         for (int f = lane; f < nf; f += 32) {
-            const int sa = f * P.node_count + n;
+            const int sa = f * NC + n;
             const float ma = B.grid_mass[sa];
             if (ma <= 0.0f) {
                 st3(B.old_v, S, sa, v3_zero());
@@ -468,14 +502,14 @@ __global__ void __launch_bounds__(256) k_p2g_multi(bm_params P, bm_buffers B, in
                 continue;
             }
             const bm_v3 pa = ld3(B.momentum, S, sa), ja = ld3(B.grid_impulse, S, sa);
-            const uint64_t oa = B.fones[sa], ta = B.ftwos[sa];
+            const uint64_t oa2 = B.fones[sa], ta2 = B.ftwos[sa];
             float total = 0.0f;
             bm_v3 dm = v3_zero(), di = v3_zero();
             for (int g = 0; g < nf; ++g) {
-                const int sb = g * P.node_count + n;
+                const int sb = g * NC + n;
                 const float mb = B.grid_mass[sb];
                 total = total + mb;
-                if (g != f && compatible_masks(oa, ta, B.fones[sb], B.ftwos[sb])) {
+                if (g != f && compatible_masks(oa2, ta2, B.fones[sb], B.ftwos[sb])) {
                     dm = v3_add(dm, v3_sub(v3_mul(ld3(B.momentum, S, sb), ma), v3_mul(pa, mb)));
                     di = v3_add(di, v3_sub(v3_mul(ld3(B.grid_impulse, S, sb), ma), v3_mul(ja, mb)));
                 }
@@ -583,81 +617,71 @@ __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B)
 }
 
 __global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) {
+    __shared__ NodeStage stage[kBlock / 32];
+    NodeStage& st = stage[threadIdx.x >> 5];
     const int count = B.flags[BM_FLAG_MULTI];
-    const int S = P.fmax * P.node_count;
-    const int lane = threadIdx.x & 31;
+    const int NC = P.node_count, S = P.fmax * NC;
+    const int lane = threadIdx.x & 31, k = lane & 3;
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < count; w += warps) {
         const int n = B.multi_nodes[w];
         const int nf = B.nfield[n];
-        const int lanef = lane >> 3, a = lane & 7;
+        const int slot = k * NC + n;
+        float ma = 0.0f;
+        uint64_t oa = 0u, ta = 0u;
+        if (nf <= 4 && k < nf) {
+            ma = B.grid_mass[slot];
+            oa = B.fones[slot];
+            ta = B.ftwos[slot];
+        }
+        stage_node<3>(P, B, n, st);
+        __syncwarp();
         for (int f0 = 0; f0 < nf; f0 += 4) {
-            const int f = f0 + lanef;
-            float val[3];
-            bool have = false;
-            if (f < nf) have = corner_value<3>(P, B, n, a, f, val);
-            if (!have) val[0] = val[1] = val[2] = 0.0f;
-            const unsigned haves = __ballot_sync(kFull, have);
-            float sum[3] = {0.0f, 0.0f, 0.0f};
-            for (int c = 7; c >= 0; --c) {
-                const int src = (lane & 24) + c;
-                const bool use = (haves >> src) & 1u;
-                for (int v = 0; v < 3; ++v) {
-                    const float x = __shfl_sync(kFull, val[v], src);
-                    if (use) sum[v] = sum[v] + x;
-                }
-            }
+            float sum[3];
+            staged_sums<3>(st, nf, f0, sum);
+            const int f = f0 + k;
             if (nf <= 4) {
                 // couple (couple_at) by shuffles, ascending field order as in the general path
-                const int sa = f * P.node_count + n;
-                float ma = 0.0f;
-                uint64_t oa = 0u, ta = 0u;
-                if (f < nf) {
-                    ma = B.grid_mass[sa];
-                    oa = B.fones[sa];
-                    ta = B.ftwos[sa];
-                }
                 const bm_v3 va = v3(sum[0], sum[1], sum[2]);
                 float total = 0.0f;
                 bm_v3 ex = v3_zero();
                 for (int g = 0; g < nf; ++g) {
-                    const int src = 8 * g;
-                    const float mb = __shfl_sync(kFull, ma, src);
-                    const bm_v3 vb = v3(__shfl_sync(kFull, va.x, src), __shfl_sync(kFull, va.y, src), __shfl_sync(kFull, va.z, src));
-                    const uint64_t ob = __shfl_sync(kFull, oa, src), tb = __shfl_sync(kFull, ta, src);
+                    const float mb = __shfl_sync(kFull, ma, g);
+                    const bm_v3 vb = v3(__shfl_sync(kFull, va.x, g), __shfl_sync(kFull, va.y, g), __shfl_sync(kFull, va.z, g));
+                    const uint64_t ob = __shfl_sync(kFull, oa, g), tb = __shfl_sync(kFull, ta, g);
                     total = total + mb;
                     if (g != f && compatible_masks(oa, ta, ob, tb)) ex = v3_add(ex, v3_sub(v3_mul(vb, ma), v3_mul(va, mb)));
                 }
-                if (a == 0 && f < nf) {
-                    st3(B.remapped, S, sa, va);
-                    if (ma <= 0.0f) st3(B.remap_v, S, sa, v3_zero());
-                    else st3(B.remap_v, S, sa, v3_div(v3_add(va, v3_div(ex, total)), ma));
+                if (lane < nf) {
+                    st3(B.remapped, S, slot, va);
+                    if (ma <= 0.0f) st3(B.remap_v, S, slot, v3_zero());
+                    else st3(B.remap_v, S, slot, v3_div(v3_add(va, v3_div(ex, total)), ma));
                 }
                 continue;
             }
-            if (a == 0 && f < nf) st3(B.remapped, S, f * P.node_count + n, v3(sum[0], sum[1], sum[2]));
+            if (lane < 4 && f < nf) st3(B.remapped, S, f * NC + n, v3(sum[0], sum[1], sum[2]));
         }
+        __syncwarp();  // the stage is rewritten for the next node; the sums are visible to the warp
         if (nf <= 4) continue;
-        __syncwarp();
         for (int f = lane; f < nf; f += 32) {
-            const int sa = f * P.node_count + n;
-            const float ma = B.grid_mass[sa];
-            if (ma <= 0.0f) {
+            const int sa = f * NC + n;
+            const float mf = B.grid_mass[sa];
+            if (mf <= 0.0f) {
                 st3(B.remap_v, S, sa, v3_zero());
                 continue;
             }
             const bm_v3 va = ld3(B.remapped, S, sa);
-            const uint64_t oa = B.fones[sa], ta = B.ftwos[sa];
+            const uint64_t oa2 = B.fones[sa], ta2 = B.ftwos[sa];
             float total = 0.0f;
             bm_v3 ex = v3_zero();
             for (int g = 0; g < nf; ++g) {
-                const int sb = g * P.node_count + n;
+                const int sb = g * NC + n;
                 const float mb = B.grid_mass[sb];
                 total = total + mb;
-                if (g != f && compatible_masks(oa, ta, B.fones[sb], B.ftwos[sb]))
-                    ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, sb), ma), v3_mul(va, mb)));
+                if (g != f && compatible_masks(oa2, ta2, B.fones[sb], B.ftwos[sb]))
+                    ex = v3_add(ex, v3_sub(v3_mul(ld3(B.remapped, S, sb), mf), v3_mul(va, mb)));
             }
-            st3(B.remap_v, S, sa, v3_div(v3_add(va, v3_div(ex, total)), ma));
+            st3(B.remap_v, S, sa, v3_div(v3_add(va, v3_div(ex, total)), mf));
         }
         __syncwarp();
     }
@@ -1067,13 +1091,32 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
     k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B, force);
 }
 
-void launch_material(const bm_solver* s, int write_sums, cudaStream_t st) {
+// Runs launch(q) on aux beside the work queued on st after this call, or on st
+// when aux is null; join_aux then makes st wait for it.
+template <class Launch>
+static void fork_aux(const bm_solver* s, cudaStream_t st, cudaStream_t aux, Launch launch) {
+    if (!aux) {
+        launch(st);
+        return;
+    }
+    cudaEventRecord(s->aux_fork, st);
+    cudaStreamWaitEvent(aux, s->aux_fork, 0);
+    launch(aux);
+    cudaEventRecord(s->aux_join, aux);
+}
+static void join_aux(const bm_solver* s, cudaStream_t st, cudaStream_t aux) {
+    if (aux) cudaStreamWaitEvent(st, s->aux_join, 0);
+}
+
+void launch_material(const bm_solver* s, int write_sums, cudaStream_t st, cudaStream_t aux) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
+    const int sums = P.viscous ? 1 : write_sums;
     k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
-    k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
-    k_p2g_multi<<<4 * 152, kBlock, 0, st>>>(P, B, P.viscous ? 1 : write_sums);
+    fork_aux(s, st, aux, [&](cudaStream_t q) { k_p2g_multi<<<4 * 152, kBlock, 0, q>>>(P, B, sums); });
+    k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, sums);
+    join_aux(s, st, aux);
     if (P.viscous) {
         // solver.py:433-459: couple momentum, velocities, viscous impulse, couple impulse, velocities.
         k_couple_slots<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, B.momentum, B.remapped);
@@ -1092,10 +1135,11 @@ void launch_g2p(const bm_solver* s, cudaStream_t st) {
     k_g2p<<<grid_for(cells8), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
 }
 
-void launch_remap(const bm_solver* s, cudaStream_t st) {
+void launch_remap(const bm_solver* s, cudaStream_t st, cudaStream_t aux) {
     const bm_params& P = s->P;
+    fork_aux(s, st, aux, [&](cudaStream_t q) { k_remap_multi<<<4 * 152, kBlock, 0, q>>>(P, s->B); });
     k_remap_couple<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, s->B);
-    k_remap_multi<<<4 * 152, kBlock, 0, st>>>(P, s->B);
+    join_aux(s, st, aux);
 }
 
 void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st) {
