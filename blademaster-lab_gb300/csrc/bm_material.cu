@@ -616,7 +616,7 @@ __global__ void __launch_bounds__(256) k_remap_couple(bm_params P, bm_buffers B)
     st3(B.remap_v, S, n, v3_div(coupled, m));
 }
 
-__global__ void __launch_bounds__(256) k_remap_multi(bm_params P, bm_buffers B) {
+__global__ void __launch_bounds__(256, 4) k_remap_multi(bm_params P, bm_buffers B) {
     __shared__ NodeStage stage[kBlock / 32];
     NodeStage& st = stage[threadIdx.x >> 5];
     const int count = B.flags[BM_FLAG_MULTI];
