@@ -143,6 +143,19 @@ MAX_BATCH = 4096
 FIELD_SLOTS = 64  # a node has at most 8 cells x 8 particles = 64 distinct codes
 
 
+def cut_capacity(node_count):
+    """The largest cut index whose codes still key every node within int64.
+
+    Cut index i sets ternary digit i, so indices 0 .. m give codes below 3^(m+1)
+    and keys code * node_count + node below node_count * 3^(m+1), which must
+    stay within 2^63 - 1 (solver.py:168-171; scripts/stress_multi_tool.py:21-43).
+    """
+    m = 0
+    while 3 ** (m + 2) * node_count <= 2**63 - 1:
+        m += 1
+    return m
+
+
 def _pow2_at_least(v):
     return 1 << (max(int(v), 1) - 1).bit_length()
 
@@ -188,9 +201,7 @@ class Solver:
         self.cells = cells
         self.node_dims = cells + 1
         self.node_count = int(np.prod(cells + 1))
-        self.max_cut_index = 0
-        while 3 ** (self.max_cut_index + 2) * self.node_count <= 2**63 - 1:
-            self.max_cut_index += 1
+        self.max_cut_index = cut_capacity(self.node_count)
         self.node_numpy, self.weight_numpy = nodes, weights
         self.gradient_numpy = gradients
         self.volume = (cfg.grid_spacing / 2) ** 3

@@ -388,6 +388,13 @@ class OracleSolver:
         for t, q in zip(targets, orientations):
             self.step(t, cutting, cut_index, q)
 
+    def drive_tool(self, target_edge, orientation=None):
+        """Solver._drive_tool (solver.py:824-831): tool.step of every knife with the current reaction sums."""
+        target = np.asarray(target_edge, np.float32).reshape(3)
+        rot = np.asarray(orientation if orientation is not None else [0, 0, 0, 1], np.float32).reshape(4)
+        for k in range(self.config.tool_count):
+            self.L.orc_drive_one(ctypes.byref(self.params), ctypes.byref(self.S), k, ptr(target), ptr(rot))
+
     def external_interval(self, state_packed, steps, cutting=True, cut_index=0):
         """ExternalToolPort.advance (coupling.py:88-189): returns (impulse, angular about the world origin, errors)."""
         self.set_cut(cut_index)

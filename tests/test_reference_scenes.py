@@ -1,0 +1,275 @@
+"""Scene tests of the reference, restated with the reference's own assertions.
+
+Each scene runs on the CPU oracle (the restated solver, float64 knife state)
+and, marked gpu, on the CUDA solver through the reference-facing API
+(Solver, ExternalToolPort, Solver._drive_tool).  The CUDA runs are compared
+bit-exactly with the oracle on the same inputs:
+
+* board penetration against the board's normal scale
+  (tests/test_board_contact.py:6-29);
+* a pitched blade resting on the board still cuts the bottom layer beside
+  its edge, leaving two pieces (tests/test_pinched_labels.py:7-35);
+* the knife servo, the free knife and the guided knife against the board,
+  and the board's edge (tests/test_tool.py:6-80);
+* the cut-code capacity follows the grid size
+  (tests/test_stress_replays.py:61-87).
+"""
+
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+from blademaster_gb300.coupling import ToolState
+from blademaster_gb300.geometry import points, stencil
+from blademaster_gb300.solver import Config, cut_capacity
+from blademaster_gb300.topology import components
+from oracle.oracle import OracleSolver
+
+
+def packed(state):
+    """The 49 floats ExternalToolPort loads for one interval (coupling.py:88-120)."""
+    s = state.checked()
+    return np.concatenate([s.position, s.orientation_xyzw, s.linear_velocity, s.angular_velocity,
+                           s.mobility.ravel()]).astype(np.float32)
+
+
+# ------------------------------------------------------------------ board
+
+def board_config(board_normal_scale):
+    return Config(size=(0.06, 0.06, 0.06), grid_spacing=0.01, dt=0.002, young_modulus=10000.0, poisson_ratio=0.4,
+                  external_tool=True, board_normal_scale=board_normal_scale)
+
+
+AWAY = ToolState([0.5, 0.0, 0.5], [0, 0, 0, 1], [0, 0, 0], [0, 0, 0])
+
+
+def settled_oracle(board_normal_scale, intervals=500):
+    c = OracleSolver(board_config(board_normal_scale))
+    for _ in range(intervals):
+        c.external_interval(packed(AWAY), 1, cutting=False)
+    return c
+
+
+@pytest.mark.parametrize("scale, bound", [(0.0, -0.003), (1.0, -0.001)])
+def test_board_penetration_follows_the_normal_scale(scale, bound):
+    # 12 particle layers settle about N g dt^2 / s_n into the board: 4.7 mm with
+    # the default s_n = 0.1, 0.5 mm with s_n = 1 (test_board_contact.py:26-29).
+    c = settled_oracle(scale)
+    x = c.get("x")
+    assert np.isfinite(x).all()
+    bottom = x[:, 2].min() - c.radius
+    assert bottom < bound if scale == 0.0 else bottom > bound
+
+
+@pytest.mark.gpu
+def test_board_penetration_cuda_matches_oracle():
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.solver import Solver
+
+    for scale in (0.0, 1.0):
+        cfg = board_config(scale)
+        g = Solver(cfg)
+        port = ExternalToolPort(g)
+        for _ in range(500):
+            port.advance(AWAY, cfg.dt, cutting=False)
+        c = settled_oracle(scale)
+        np.testing.assert_array_equal(g.x.numpy(), c.get("x"))
+        np.testing.assert_array_equal(g.v.numpy(), c.get("v"))
+
+
+# --------------------------------------------------- pitched edge on board
+
+PINCH = Config(size=(0.06, 0.03, 0.03), grid_spacing=0.006, dt=0.00025, sampling_seed=1, external_tool=True,
+               board_normal_scale=1.0, blade_half_size=(0.0005, 0.025, 0.02))
+
+
+def pinch_states(intervals=1000):
+    """The knife pitched 10 degrees about its length axis, descending at 0.05 m/s
+    to 0.2 mm above the board, then held (test_pinched_labels.py:21-30)."""
+    pitch = np.deg2rad(10.0)
+    q = [0.0, np.sin(pitch / 2), 0.0, np.cos(pitch / 2)]
+    reach = PINCH.blade_half_size[2] * np.cos(pitch)
+    lean = PINCH.blade_half_size[2] * np.sin(pitch)
+    interval, speed, start, stop = 0.001, 0.05, 0.04, 0.0002
+    for i in range(intervals):
+        edge = max(start - speed * i * interval, stop)
+        moving = edge > stop
+        yield ToolState([lean, 0.0, edge + reach], q, [0.0, 0.0, -speed if moving else 0.0], [0, 0, 0])
+
+
+def assert_pinched_cut(codes, x, node_numpy, weight_numpy):
+    assert not ((codes == 0) & (np.abs(x[:, 0]) < 2 * PINCH.grid_spacing)).any()
+    _, sizes = components(node_numpy, weight_numpy, codes)
+    assert len(sizes) == 2
+
+
+def test_pitched_edge_on_the_board_cuts_the_bottom_layer():
+    c = OracleSolver(PINCH)
+    for state in pinch_states():
+        c.external_interval(packed(state), 4, cutting=True, cut_index=0)
+    assert_pinched_cut(c.get("codes"), c.get("x"), c.node_numpy, c.weight_numpy)
+
+
+@pytest.mark.gpu
+def test_pitched_edge_cuda_matches_oracle_and_cuts():
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.solver import Solver
+
+    g = Solver(PINCH)
+    port = ExternalToolPort(g)
+    c = OracleSolver(PINCH)
+    for i, state in enumerate(pinch_states()):
+        port.advance(state, 0.001, cutting=True)
+        if i < 200:
+            c.external_interval(packed(state), 4, cutting=True, cut_index=0)
+        if i == 199:
+            for name in ("x", "v", "codes", "damage"):
+                np.testing.assert_array_equal(getattr(g, name).numpy(), c.get(name), err_msg=name)
+    assert_pinched_cut(g.codes.numpy(), g.x.numpy(), g.node_numpy, g.weight_numpy)
+
+
+# ------------------------------------------------------------- knife drive
+
+BLADE_CORNERS = np.array([[0.0, -1.0, -1.0], [0.0, 1.0, -1.0], [1.0, -1.0, -1.0], [-1.0, 1.0, -1.0]])
+
+
+def lowest_vertex(cfg, pos, rot):
+    """Height of the knife's lowest wedge vertex (test_tool.py:6-14)."""
+    from scipy.spatial.transform import Rotation
+
+    h, bevel = np.array(cfg.blade_half_size), cfg.blade_bevel_height
+    vertices = BLADE_CORNERS * [h[0], h[1], h[2]] + [[0, 0, 0], [0, 0, 0], [0, 0, bevel], [0, 0, bevel]]
+    return (Rotation.from_quat(rot).apply(vertices) + pos)[:, 2].min()
+
+
+class OracleDriver:
+    def __init__(self, cfg):
+        self.cfg, self.s = cfg, OracleSolver(cfg)
+
+    def place(self, pos, rot=None):
+        self.s.set("tool_pos", [pos])
+        if rot is not None:
+            self.s.set("tool_rot", [rot])
+
+    def drive(self, target, rot):
+        self.s.drive_tool(target, rot)
+
+    def state(self):
+        return (self.s.get("tool_pos")[0], self.s.get("tool_rot")[0], self.s.get("tool_vel")[0],
+                self.s.get("table_impulse")[0])
+
+
+class CudaDriver:
+    def __init__(self, cfg):
+        from blademaster_gb300.solver import Solver
+
+        self.cfg, self.s = cfg, Solver(cfg)
+
+    def place(self, pos, rot=None):
+        self.s.tool_pos.assign([pos])
+        if rot is not None:
+            self.s.tool_rot.assign([rot])
+
+    def drive(self, target, rot):
+        self.s._drive_tool(target, rot, None, None, 0)
+
+    def state(self):
+        s = self.s
+        return s.tool_pos.numpy()[0], s.tool_rot.numpy()[0], s.tool_vel.numpy()[0], s.tool_table_impulse.numpy()[0]
+
+
+def drive(d, target, rot, steps=3000):
+    """test_tool.py:17-24: the lowest vertex every 20 tool steps."""
+    lowest = []
+    for i in range(steps):
+        d.drive(target, rot)
+        if i % 20 == 0:
+            pos, q, _, _ = d.state()
+            lowest.append(lowest_vertex(d.cfg, np.asarray(pos, float), np.asarray(q, float)))
+    assert np.isfinite(d.state()[2]).all()
+    return np.array(lowest)
+
+
+TILT = 0.2
+TILTED = np.array([0.0, np.sin(TILT / 2), 0.0, np.cos(TILT / 2)])
+
+
+def tool_config(free):
+    return replace(Config(), dt=0.00025, pose_servo=not free, free_blade=free, blade_bevel_height=0.005)
+
+
+def run_tool(driver, free):
+    d = driver(tool_config(free))
+    d.place([0.12, 0.0, 0.05], TILTED)
+    lowest = drive(d, [0.12, 0.0, -0.01], TILTED)
+    assert lowest.min() > -2e-5
+    assert lowest.max() - lowest.min() > 0.01
+    return d
+
+
+def guided(driver):
+    d = driver(replace(Config(), dt=0.00025, blade_bevel_height=0.005))
+    d.place([0.0, 0.0, 0.05])
+    lowest = drive(d, [0.0, 0.0, -0.01], [0.0, 0.0, 0.0, 1.0])
+    assert lowest.min() > -2e-5 and lowest[-1] < 1e-4
+    return d
+
+
+def board_edge(driver):
+    cfg = replace(Config(), dt=0.00025, free_blade=True, board_half_extent=(0.05, 0.05))
+    on, off = driver(cfg), driver(cfg)
+    on.place([0.0, 0.0, 0.05])
+    off.place([0.2, 0.0, 0.05])
+    assert drive(on, [0, 0, 0], [0, 0, 0, 1], 1500).min() > -2e-5
+    assert drive(off, [0, 0, 0], [0, 0, 0, 1], 1500).min() < -0.05
+    return on, off
+
+
+def test_six_dof_servo_rests_on_the_board():
+    pos, _, _, table = run_tool(OracleDriver, free=False).state()
+    assert pos[2] > 0.018
+    assert table[2] > 0
+
+
+def test_free_knife_falls_onto_the_board():
+    run_tool(OracleDriver, free=True)
+
+
+def test_guided_knife_stops_on_the_board_without_rotating():
+    _, rot, _, table = guided(OracleDriver).state()
+    np.testing.assert_allclose(rot, [0, 0, 0, 1], atol=1e-7)
+    assert table[2] > 0
+
+
+def test_board_contact_ends_at_the_board_edge():
+    board_edge(OracleDriver)
+
+
+@pytest.mark.gpu
+def test_knife_drives_cuda_match_oracle():
+    pairs = [(run_tool(CudaDriver, free), run_tool(OracleDriver, free)) for free in (False, True)]
+    pairs.append((guided(CudaDriver), guided(OracleDriver)))
+    pairs.extend(zip(board_edge(CudaDriver), board_edge(OracleDriver)))
+    for g, c in pairs:
+        for a, b in zip(g.state(), c.state()):
+            np.testing.assert_array_equal(np.asarray(a), np.asarray(b).astype(np.asarray(a).dtype))
+
+
+# --------------------------------------------------------------- capacity
+
+@pytest.mark.parametrize("spacing, nodes", [(0.015, 45), (0.0075, 225), (0.00375, 1377)])
+def test_capacity_follows_the_reference_geometry(spacing, nodes):
+    # tests/test_stress_replays.py:72-80 and 61-69
+    cfg = Config(grid_spacing=spacing)
+    reference, origin, cells = points(cfg.size, cfg.grid_spacing, cfg.shape, cfg.sampling_seed)
+    node_ids, _, _ = stencil(reference, origin, cfg.grid_spacing, cells)
+    assert int(np.prod(cells + 1)) == nodes
+    assert node_ids.min() == 0 and node_ids.max() + 1 == nodes
+    digits = cut_capacity(nodes) + 1
+    # every code of `digits` ternary digits keys every node within int64, one more digit would not
+    assert nodes * 3**digits - 1 <= np.iinfo(np.int64).max < nodes * 3 ** (digits + 1) - 1
+    if nodes == 225:
+        assert digits == 34  # test_stress_replays.py:51-53
+    else:
+        assert digits != 34
