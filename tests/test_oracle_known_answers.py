@@ -9,7 +9,10 @@ restatements written in this file, independently of oracle/oracle.c:
 * Eq. 8 field exchange as a dense matrix product over a compatibility mask;
 * the blade's signed distance as the distance to a convex polygon extruded
   along y (a different construction from the reference's feature walk);
-* the stick/slip friction law in float64.
+* the stick/slip friction law in float64;
+* one TLMPM material step (P2G over (node, code) fields, Eq. 8, grid
+  velocities, G2P with Eq. 13 advection, the MUSL re-scatter and the F
+  update with the corotated stress from a float64 SVD), as dense numpy.
 
 These tests never touch a GPU.
 """
@@ -200,6 +203,92 @@ def test_friction_stick_and_slip_history():
 
 
 # --------------------------------------------------------------- plasticity
+
+
+def corotated_fp64(F, mu, lam):
+    """P = 2 mu (F - R) + lam (J - 1) J F^-T with R = U V^T from the SVD (Fp = I)."""
+    U, _, Vt = np.linalg.svd(F)
+    R = U @ Vt
+    J = np.linalg.det(F)
+    return 2.0 * mu * (F - R) + (lam * (J - 1.0) * J)[:, None, None] * np.linalg.inv(F).transpose(0, 2, 1)
+
+
+def material_step_fp64(x, v, F, codes, nodes, w, g, imp, mass, volume, mu, lam, dt, flip, node_count, viscosity):
+    """One material step (solver.py:334-376, 431-535) in float64: fields are the
+    distinct (node, code) keys of every particle's 8 stencil nodes."""
+    n = len(x)
+    keys = codes[:, None] * node_count + nodes
+    unique, slot = np.unique(keys, return_inverse=True)
+    slot = slot.reshape(n, 8)
+    S = len(unique)
+    node_of, code_of = unique % node_count, unique // node_count
+    same = node_of[:, None] == node_of[None, :]
+    compat = np.array([[compatible(int(a), int(b)) for b in code_of] for a in code_of]) & same
+    np.fill_diagonal(compat, False)
+    P = corotated_fp64(F, mu, lam)
+    m = np.zeros(S)
+    mom = np.zeros((S, 3))
+    J = np.zeros((S, 3))
+    np.add.at(m, slot, mass * w)
+    np.add.at(mom, slot, mass * w[..., None] * v[:, None, :])
+    np.add.at(J, slot, w[..., None] * imp[:, None, :] - dt * volume * np.einsum("pij,paj->pai", P, g))
+    node_mass = np.zeros(node_count)
+    np.add.at(node_mass, node_of, m)
+    total = node_mass[node_of]
+
+    def couple(state):  # Eq. 8 over the compatible fields of each node
+        return state + (m[:, None] * (compat @ state) - (compat @ m)[:, None] * state) / total[:, None]
+
+    pc = couple(mom)
+    if viscosity:
+        old_v = pc / m[:, None]
+        rate = np.einsum("pai,paj->pij", old_v[slot], g)
+        inv = np.linalg.inv(F)
+        L = rate @ inv
+        sigma = viscosity * np.linalg.det(F)[:, None, None] * (L + L.transpose(0, 2, 1)) @ inv.transpose(0, 2, 1)
+        np.add.at(J, slot, -dt * volume * np.einsum("pij,paj->pai", sigma, g))
+    old_v = pc / m[:, None]
+    new_v = (pc + couple(J)) / m[:, None]
+    pic = np.einsum("pa,pai->pi", w, new_v[slot])
+    dv = np.einsum("pa,pai->pi", w, (new_v - old_v)[slot])
+    v_new = (1.0 - flip) * pic + flip * (v + dv)
+    x_new = x + dt * pic
+    remapped = np.zeros((S, 3))
+    np.add.at(remapped, slot, mass * w[..., None] * v_new[:, None, :])
+    velocity = couple(remapped) / m[:, None]
+    F_new = F + dt * np.einsum("pai,paj->pij", velocity[slot], g)
+    return x_new, v_new, F_new
+
+
+@pytest.mark.parametrize("viscosity", [0.0, 2.0])
+def test_material_step_against_fp64_and_momentum(viscosity):
+    # tests/test_mechanics.py:183-225: two incompatible pieces (codes 1 | 2 across x = 0)
+    # under a stretch, random velocities and contact impulses; the reference's tolerances.
+    cfg = replace(Config(), dynamic_viscosity=viscosity)
+    c = OracleSolver(cfg)
+    rng = np.random.default_rng(4)
+    vel = rng.normal(scale=0.01, size=(c.n, 3)).astype(F32)
+    F = np.tile(np.diag([1.01, 0.995, 1.0]), (c.n, 1, 1)).astype(F32)
+    codes = np.where(c.reference[:, 0] < 0, 1, 2).astype(np.int64)
+    impulse = rng.normal(scale=1e-8, size=(c.n, 3)).astype(F32)
+    c.set("v", vel)
+    c.set("F", F)
+    c.refresh_stress()
+    c.set("codes", codes)
+    c.set("impulses", impulse)
+    x = c.get("x").astype(float)
+    reference, origin, cells = points(cfg.size, cfg.grid_spacing, cfg.shape, cfg.sampling_seed)
+    nodes, w, g = stencil(reference, origin, cfg.grid_spacing, cells)
+    expect = material_step_fp64(x, vel.astype(float), F.astype(float), codes, nodes.astype(np.int64),
+                                w.astype(F32).astype(float), g.astype(F32).astype(float), impulse.astype(float),
+                                c.mass, c.volume, c.mu, c.lam, cfg.dt, cfg.flip_fraction, c.node_count, viscosity)
+    before = c.mass * vel.astype(float).sum(0)
+    c.material_step()
+    np.testing.assert_allclose(c.get("x"), expect[0], atol=1e-8)
+    np.testing.assert_allclose(c.get("v"), expect[1], atol=2e-6)
+    np.testing.assert_allclose(c.get("F"), expect[2], atol=2e-6)
+    np.testing.assert_allclose(c.mass * c.get("v").astype(float).sum(0), before + impulse.astype(float).sum(0),
+                               atol=2e-9)
 
 
 def test_von_mises_projection_preserves_total_and_volume():
