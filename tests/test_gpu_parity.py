@@ -101,6 +101,7 @@ def test_ragged_particle_count_cut_is_bitexact():
 
 
 def test_graph_replay_is_bitexact_with_eager_and_oracle():
+    # tests/test_graph.py:6-30: odd/even batches (both history buffers), a pause and a new cut
     cfg = replace(Config(), free_blade=True)
     eager, graphed = Solver(cfg), Solver(cfg)
     c = OracleSolver(cfg)
@@ -122,7 +123,8 @@ def test_graph_replay_is_bitexact_with_eager_and_oracle():
 def test_gated_chains_in_graphs_match_eager_launches(cache_topology):
     """The full pair-list build, the incremental relist and (with a cached
     topology) the registration are gated on device flags; a replayed graph
-    and eager launches run each of them equally often, with equal results."""
+    and eager launches run each of them equally often, with equal results
+    (tests/test_graph.py:6-30 and tests/test_topology_cache.py:6-20 on one scene)."""
     from blademaster_gb300 import _native
 
     cfg = replace(Config(), cache_topology=cache_topology)

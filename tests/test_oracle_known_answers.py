@@ -291,6 +291,50 @@ def test_material_step_against_fp64_and_momentum(viscosity):
                                atol=2e-9)
 
 
+def test_cut_labels_persist_through_withdrawal_and_a_new_cut():
+    # tests/test_mechanics.py:228-300: side labels of digit 3^0 under the knife; a withdrawn
+    # knife changes nothing; a second cut with digit 3^1 keeps the first digit of every code.
+    c = OracleSolver(Config())
+    c.set("tool_pos", [[0.0, 0.0, 0.03]])
+    c.assign_sides(0, True)
+    first = c.get("codes").copy()
+    assert set(np.unique(first)) == {0, 1, 2}
+    c.set("tool_pos", [[0.02, 0.0, 0.1]])
+    c.assign_sides(0, True)
+    np.testing.assert_array_equal(c.get("codes"), first)
+    c.set("tool_pos", [[0.012, 0.0, 0.03]])
+    c.assign_sides(1, True)
+    np.testing.assert_array_equal(c.get("codes") % 3, first)
+    assert c.get("codes").max() > 2
+
+
+def test_cached_topology_rebuilds_on_new_labels_and_equals_uncached():
+    # tests/test_topology_cache.py:6-20; the oracle is deterministic, so the two agree exactly.
+    plain, cached = OracleSolver(Config()), OracleSolver(replace(Config(), cache_topology=True))
+    for c in (plain, cached):
+        c.set("tool_pos", [[0.0, 0.0, 0.047]])
+    for count, cut, on in [(8, 0, True), (8, 0, True), (8, 0, False), (7, 1, True), (8, 1, True)]:
+        targets = np.tile([0.0, 0.0, 0.019], (count, 1))
+        plain.advance(targets, cutting=on, cut_index=cut)
+        cached.advance(targets, cutting=on, cut_index=cut)
+        for name in ("codes", "x", "v", "F"):
+            np.testing.assert_array_equal(plain.get(name), cached.get(name), err_msg=name)
+    assert np.count_nonzero(cached.get("codes")) > 0
+
+
+def test_unmodified_material_keeps_cached_slots():
+    # tests/test_topology_cache.py:23-31
+    from blademaster_gb300 import _native
+
+    c = OracleSolver(replace(Config(), cache_topology=True))
+    c.advance(np.tile([0.0, 0.0, 1.0], (2, 1)), cutting=False)
+    slots, keys = c.get("slots").copy(), c.get("keys").copy()
+    c.advance(np.tile([0.0, 0.0, 1.0], (2, 1)), cutting=False)
+    np.testing.assert_array_equal(c.get("slots"), slots)
+    np.testing.assert_array_equal(c.get("keys"), keys)
+    assert c.get("flags")[_native.FLAG["TOPOLOGY_DIRTY"]] == 0
+
+
 def test_von_mises_projection_preserves_total_and_volume():
     # tests/test_mechanics.py:303-314
     s = OracleSolver(Config())
