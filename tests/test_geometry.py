@@ -54,3 +54,43 @@ def test_empty_and_clipped_domains():
     x, _, _ = points((0.12, 0.036, 0.036), 0.006, "hcylinder")
     assert len(x) > 0 and (levelset(x, (0.12, 0.036, 0.036), "hcylinder") <= 0).all()
     assert x[:, 2].min() > 0 and abs(np.ptp(x[:, 0]) - 0.117) < 1e-9
+
+
+# tests/test_geometry.py of the reference: the sampling rules themselves
+
+
+def test_banana_is_not_silently_clipped():
+    # test_geometry.py:6-13
+    with pytest.raises(ValueError, match="clipped"):
+        points((0.072, 0.024, 0.03), 0.006, "banana")
+    a, _, _ = points((0.072, 0.06, 0.03), 0.006, "banana")
+    b, _, _ = points((0.072, 0.072, 0.03), 0.006, "banana")
+    np.testing.assert_allclose(a, b)
+    assert len(a) == 892
+    assert (levelset(a, (0.072, 0.06, 0.03), "banana") <= 0).all()
+
+
+@pytest.mark.parametrize("spacing", [0.004, 0.007])
+def test_spacing_that_does_not_divide_the_size_still_covers_the_banana(spacing):
+    # test_geometry.py:16-29
+    from blademaster_gb300.geometry import BANANA_DEMO_SIZE_M
+
+    size = np.array(BANANA_DEMO_SIZE_M)
+    fine, _, _ = points(size, 0.003, "banana")
+    x, origin, cells = points(size, spacing, "banana")
+    assert np.all(cells * spacing >= size - 1.0e-12)
+    assert np.all((x >= origin) & (x <= origin + cells * spacing))
+    assert abs(np.ptp(x[:, 0]) - np.ptp(fine[:, 0])) < spacing / 2
+    block, origin, _ = points((0.03, 0.03, 0.03), spacing, "block")
+    assert np.all(block - origin <= 0.03)
+
+
+@pytest.mark.parametrize("shape", ["banana", "block"])
+def test_jittered_particles_start_clear_of_the_board(shape):
+    # test_geometry.py:32-39
+    from blademaster_gb300.geometry import BANANA_DEMO_SIZE_M
+
+    size = BANANA_DEMO_SIZE_M if shape == "banana" else (0.06, 0.03, 0.03)
+    for seed in (1, 2):
+        x, _, _ = points(size, 0.006, shape, seed)
+        assert x[:, 2].min() >= 0.006 / 4
