@@ -10,14 +10,16 @@ measures on no dataset).
 
 One step = one substep over every particle.  `value` times K substeps
 replayed as CUDA graphs with all state resident in HBM; `e2e` times the
-public API (Solver.advance, one substep per call) with the knife target
-copied from pinned host memory and the knife state read back every step.
+public API over the same substeps (Solver.advance, one batch of substeps per
+call) with the knife target copied from pinned host memory and the knife
+state read back every call; `e2e_single_substep` does the same with one
+substep per call.
 The CPU baseline runs the C oracle (the reference's algorithm restated, all
 host threads) on a bounded number of substeps of the same workload.
 
 --impl reference times that CPU restatement alone, on the same workload and
-metric (the reference's own implementation, Warp 1.18, is not installed on
-the GPU machine and refuses CPU devices, blademaster_warp/solver.py:161-162).
+metric (the reference's own implementation needs Warp 1.18, which is not
+installed, and refuses CPU devices, blademaster_warp/solver.py:161-162).
 """
 
 import argparse

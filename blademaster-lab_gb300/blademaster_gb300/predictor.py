@@ -8,7 +8,7 @@ particles around the edge; the output is the interval's force and torque
 activations, fp32 accumulation.  Every GEMM of training and inference runs on
 the tensor cores through bm_gemm_tn_bf16 (tcgen05); the elementwise steps
 (transposes, ReLU backward, loss gradient, bias sums, Adam) are the library's
-own kernels.  The plain substeps stay the judge: ``GatedPredictor`` accepts a
+own kernels.  The plain substeps stay the referee: ``GatedPredictor`` accepts a
 prediction only within 1 % of the plain interval's wrench.
 """
 
@@ -224,7 +224,7 @@ def features(solver, state, material_top):
 
 
 class GatedPredictor:
-    """The plain substeps as the judge of the predictor (1 % wrench tolerance).
+    """The plain substeps as the referee of the predictor (1 % wrench tolerance).
 
     ``advance`` predicts the interval's wrench, runs the plain interval through
     the port, and accepts the prediction only if the force and torque are each

@@ -754,8 +754,8 @@ __device__ void pair_particle(const bm_params& P, const bm_buffers& B, int p, fl
             }
         }
     } else {
-        // More partners than lanes: the buckets of this build at the build
-        // position, visited in ascending particle order by repeated selection.
+        // More partners than lanes: the buckets of the last list rebuild at the
+        // rebuild position, visited in ascending particle order by repeated selection.
         const bm_v3 bx = ld3(B.built_x, N, p);
         const int hx = cell_coord(bx.x, reach), hy = cell_coord(bx.y, reach), hz = cell_coord(bx.z, reach);
         int last = -1;
