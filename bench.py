@@ -260,6 +260,121 @@ def run_sweep(args, rank, world):
         dist.destroy_process_group()
 
 
+def run_learned(args, rank, world):
+    """The learned tool predictor against the plain intervals it stands in for.
+
+    Instances of the horizontal-cylinder sweep at 6 mm advance together, one
+    1 ms coupling interval (16 substeps) per batched graph launch.  After the
+    warm-up intervals, even intervals give training rows (predictor features
+    at the interval's start, the plain interval's wrench) and odd intervals
+    are held out.  The MLP (tcgen05 GEMMs) trains on the even rows.  On each
+    held-out interval the plain interval is the referee: a prediction is
+    accepted when force and torque are each within 1 % of the plain ones.
+    `value` is the learned path's throughput on the held-out intervals: their
+    particle-substeps over the time of feature extraction and inference for
+    every instance plus the plain interval for the rejected share of the
+    instances (that share of the batched interval's time).  `plain` is the
+    batched plain intervals alone.
+    """
+    import torch
+
+    from blademaster_gb300 import replicas
+    from blademaster_gb300.batch import SolverBatch
+    from blademaster_gb300.predictor import ToolPredictor, features
+    from blademaster_gb300.sweep import RADIUS, instances
+    from blademaster_gb300.solver import Solver
+
+    dist, rank, world, local = replicas.init()
+    torch.cuda.set_device(local)
+    count = args.learned_instances
+    everything = instances(count * world, seed=11, spacings=(0.006,))
+    sweep = [everything[i] for i in replicas.shard(len(everything), rank, world)]
+    solvers = [Solver(i.config, device=f"cuda:{local}") for i in sweep]
+    batch = SolverBatch(solvers, lanes=len(solvers))
+    steps = [int(round(0.001 / s.config.dt)) for s in solvers]
+    work = sum(s.n * k for s, k in zip(solvers, steps))  # particle-substeps of one interval of every instance
+    top = 2 * RADIUS
+
+    def sync():
+        torch.cuda.synchronize(local)
+
+    def interval(k):
+        """Features at the interval's start, the plain wrenches, and the two times."""
+        states = [i.state(k, start_gap=-0.0005) for i in sweep]
+        sync()
+        t0 = time.perf_counter()
+        x = np.array([features(s, st, top) for s, st in zip(solvers, states)])
+        sync()
+        t1 = time.perf_counter()
+        reactions = batch.advance(states, 0.001, strict=False)
+        sync()
+        t2 = time.perf_counter()
+        y = np.array([np.concatenate([r.impulse_ns, r.angular_impulse_nms]) / 0.001 for r in reactions])
+        return x, y, t1 - t0, t2 - t1
+
+    for k in range(args.warmup):
+        interval(k)
+    train_x, train_y, held = [], [], []
+    for j in range(2 * args.steps):
+        x, y, t_features, t_plain = interval(args.warmup + j)
+        if j % 2 == 0:
+            train_x.append(x)
+            train_y.append(y)
+        else:
+            held.append((x, y, t_features, t_plain))
+    predictor = ToolPredictor(device=f"cuda:{local}", seed=0)
+    history = predictor.fit(np.concatenate(train_x), np.concatenate(train_y), epochs=args.learned_epochs, batch=64,
+                            lr=2e-3)
+    predictor.predict(held[0][0])  # first call outside the timing
+    learned_s = plain_s = 0.0
+    accepted = total = 0
+    force_err, torque_err, mean_err = [], [], []
+    mean = np.concatenate(train_y).mean(0)
+    for x, y, t_features, t_plain in held:
+        sync()
+        t0 = time.perf_counter()
+        predicted = predictor.predict(x)
+        sync()
+        t_infer = time.perf_counter() - t0
+        fe = np.linalg.norm(predicted[:, :3] - y[:, :3], axis=1) / np.maximum(np.linalg.norm(y[:, :3], axis=1), 1e-12)
+        te = np.linalg.norm(predicted[:, 3:] - y[:, 3:], axis=1) / np.maximum(np.linalg.norm(y[:, 3:], axis=1), 1e-12)
+        ok = (fe <= 0.01) & (te <= 0.01)
+        force_err.extend(fe.tolist())
+        torque_err.extend(te.tolist())
+        mean_err.extend((np.linalg.norm(mean[:3] - y[:, :3], axis=1) /
+                         np.maximum(np.linalg.norm(y[:, :3], axis=1), 1e-12)).tolist())
+        accepted += int(ok.sum())
+        total += len(ok)
+        learned_s += t_features + t_infer + (1.0 - ok.mean()) * t_plain
+        plain_s += t_plain
+    learned_s = replicas.max_over_ranks(dist, learned_s)
+    plain_s = replicas.max_over_ranks(dist, plain_s)
+    held_work = replicas.sum_over_ranks(dist, work * len(held))
+    accepted = replicas.sum_over_ranks(dist, accepted)
+    total = replicas.sum_over_ranks(dist, total)
+    particles = replicas.sum_over_ranks(dist, sum(s.n for s in solvers))
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": held_work / learned_s, "unit": UNIT, "n_gpus": world, "steps": len(held),
+            "warmup": args.warmup, "ms_per_step": learned_s / len(held) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (MLP) + f32 (plain referee)", "data": "synthetic",
+            "config": {"workload": f"learned_{count}_hcylinders_6mm", "instances": count, "particles": int(particles),
+                       "substeps_per_interval": steps[0], "training_intervals": len(train_x),
+                       "held_out_intervals": len(held), "epochs": args.learned_epochs,
+                       "step": "one held-out 1 ms interval of every instance: features, MLP, and the plain "
+                               "interval for the rejected share"},
+            "plain": {"value": held_work / plain_s, "ms_per_step": plain_s / len(held) * 1e3},
+            "learned": {"acceptance": accepted / max(total, 1), "tolerance": 0.01,
+                        "force_rel_err_median": float(np.median(force_err)),
+                        "torque_rel_err_median": float(np.median(torque_err)),
+                        "mean_predictor_force_rel_err_median": float(np.median(mean_err)),
+                        "training_loss": [float(history[0]), float(history[-1])]},
+            "parallelism": f"replicas x{world}, {count} instances per rank",
+        }), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -300,6 +415,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="launch substeps without CUDA graphs (profiling)")
     ap.add_argument("--instances", type=int, default=256, help="instances of the sweep_c4 workload")
+    ap.add_argument("--learned-instances", type=int, default=64, help="instances of the learned_c5 workload")
+    ap.add_argument("--learned-epochs", type=int, default=80, help="training epochs of the learned_c5 predictor")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -311,6 +428,9 @@ def main():
         return
     if args.workload == "sweep_c4":
         run_sweep(args, rank, world)
+        return
+    if args.workload == "learned_c5":
+        run_learned(args, rank, world)
         return
 
     import torch
