@@ -335,6 +335,26 @@ def test_unmodified_material_keeps_cached_slots():
     assert c.get("flags")[_native.FLAG["TOPOLOGY_DIRTY"]] == 0
 
 
+def test_codes_at_full_capacity_register_without_overflow():
+    # tests/test_stress_replays.py:44-58: 225 nodes keep 34 ternary digits; the highest
+    # code 3^34 - 1 at the last node gives the highest key 225 * 3^34 - 1 < 2^63.
+    c = OracleSolver(Config())
+    assert c.node_count == 225
+    rng = np.random.default_rng(7)
+    codes = rng.integers(0, 3**34, c.n, dtype=np.int64)
+    nodes = c.node_numpy.astype(np.int64)
+    last = int(np.argmax(nodes.max(1)))
+    codes[last] = 3**34 - 1
+    c.set("codes", codes)
+    c.register()
+    keys = c.get("keys")
+    expected = np.unique(codes[:, None] * 225 + nodes)
+    np.testing.assert_array_equal(np.sort(keys[keys >= 0]), expected)
+    assert keys.max() == 225 * 3**34 - 1
+    np.testing.assert_array_equal(keys[c.get("slots")][c.rank], codes[:, None] * 225 + nodes)
+    assert not c.get("errors").any()
+
+
 def test_von_mises_projection_preserves_total_and_volume():
     # tests/test_mechanics.py:303-314
     s = OracleSolver(Config())
