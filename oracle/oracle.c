@@ -644,7 +644,7 @@ static void hold_constraint(const bm_params* P, orc_state* S) {
     int needs = 0, batches = 0, a;
     float residual = 0.0f;
     for (p = 0; p < n; ++p) {
-        bm_v3 local = q_rotate_inv(T.rot, v3_sub(ld3(S->x, p), T.pos)), grid_v = v3_zero(), nn, g;
+        bm_v3 local = q_rotate_inv(T.rot, v3_sub(ld3(S->x, p), T.pos)), grid_v = v3_zero(), nn;
         float side, gap;
         if (fabsf(local.y) >= P->half[1] || local.z <= -P->half[2] + P->bevel || local.z >= P->half[2]) {
             S->hold_side[p] = 0.0f;
@@ -1155,11 +1155,6 @@ static int64_t list_bucket(int64_t cx, int64_t cy, int64_t cz, int64_t mask) {
                      (uint32_t)mask);
 }
 
-static int cmp_i64(const void* a, const void* b) {
-    int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
-    return x < y ? -1 : (x > y ? 1 : 0);
-}
-
 /* Solver.particle_contacts (solver.py:670-751): clear_pair_slots, then every
  * pair within 2 radius + 2 dt speed (the hash search reach, contact.py:684)
  * through pair_at.  Partners of a particle are visited in ascending order. */
@@ -1173,33 +1168,43 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
     for (i = 0; i < S->pair_count[nw]; ++i)
         S->pair_keys[(int64_t)nw * P->pair_capacity + S->pair_used[(int64_t)nw * P->pair_capacity + i]] = -1;
     S->pair_count[nw] = 0;
+    /* each particle's cell, once (the candidate test below compares cells) */
+    int64_t* cell = (int64_t*)malloc(sizeof(int64_t) * 3 * (size_t)(n > 0 ? n : 1));
+    for (p = 0; p < n; ++p) {
+        bm_v3 xp = ld3(S->x, p);
+        cell[3 * p] = cell_coord(xp.x, reach);
+        cell[3 * p + 1] = cell_coord(xp.y, reach);
+        cell[3 * p + 2] = cell_coord(xp.z, reach);
+    }
     for (i = 0; i < S->buckets; ++i) S->cell_head[i] = -1;
     for (p = n - 1; p >= 0; --p) {
-        bm_v3 xp = ld3(S->x, p);
-        int64_t b = list_bucket(cell_coord(xp.x, reach), cell_coord(xp.y, reach), cell_coord(xp.z, reach), mask);
+        int64_t b = list_bucket(cell[3 * p], cell[3 * p + 1], cell[3 * p + 2], mask);
         S->cell_next[p] = S->cell_head[b];
         S->cell_head[b] = (int32_t)p;
     }
 #pragma omp parallel
     {
     int64_t* list = (int64_t*)malloc(sizeof(int64_t) * 4096);
-#pragma omp for schedule(dynamic, 1024) reduction(+ : err0, err2)
+#pragma omp for schedule(dynamic, 64) reduction(+ : err0, err2)
     for (p = 0; p < n; ++p) {
-        bm_v3 xp = ld3(S->x, p), total = ld3(S->impulses, p);
-        int64_t cx = cell_coord(xp.x, reach), cy = cell_coord(xp.y, reach), cz = cell_coord(xp.z, reach), count = 0;
+        bm_v3 total = ld3(S->impulses, p);
+        int64_t cx = cell[3 * p], cy = cell[3 * p + 1], cz = cell[3 * p + 2], count = 0, u, w;
         int c, touched = 0;
         for (c = 0; c < 27; ++c) {
             int64_t nx = cx + c % 3 - 1, ny = cy + (c / 3) % 3 - 1, nz = cz + c / 9 - 1;
             int32_t q = S->cell_head[list_bucket(nx, ny, nz, mask)];
             for (; q >= 0; q = S->cell_next[q]) {
-                bm_v3 xq = ld3(S->x, q);
                 if (q == p) continue;
-                if (cell_coord(xq.x, reach) != nx || cell_coord(xq.y, reach) != ny || cell_coord(xq.z, reach) != nz)
-                    continue;
+                if (cell[3 * q] != nx || cell[3 * q + 1] != ny || cell[3 * q + 2] != nz) continue;
                 if (count < 4096) list[count++] = q;
             }
         }
-        qsort(list, (size_t)count, sizeof(int64_t), cmp_i64);
+        /* ascending partner order (insertion sort: the lists are short) */
+        for (u = 1; u < count; ++u) {
+            int64_t v = list[u];
+            for (w = u; w > 0 && list[w - 1] > v; --w) list[w] = list[w - 1];
+            list[w] = v;
+        }
         for (int64_t li = 0; li < count; ++li) {
             bm_v3 j;
             if (pair_impulse(P, S, p, list[li], old, nw, &j, &err0, &err2)) {
@@ -1211,6 +1216,7 @@ ORC_API void orc_particle_contacts(const bm_params* P, orc_state* S) {
     }
     free(list);
     }
+    free(cell);
     S->errors[0] += err0;
     S->errors[2] += err2;
 }

@@ -12,7 +12,9 @@ bit-exactly with the oracle on the same inputs:
 * the knife servo, the free knife and the guided knife against the board,
   and the board's edge (tests/test_tool.py:6-80);
 * the cut-code capacity follows the grid size
-  (tests/test_stress_replays.py:61-87).
+  (tests/test_stress_replays.py:61-87);
+* a cut at index 25 (digit 3^25, beyond 32 bits) severs the banana into two
+  pieces (tests/test_coupling.py:131-145).
 """
 
 from dataclasses import replace
@@ -273,3 +275,25 @@ def test_capacity_follows_the_reference_geometry(spacing, nodes):
         assert digits == 34  # test_stress_replays.py:51-53
     else:
         assert digits != 34
+
+
+# ------------------------------------------------------------- deep digit
+
+def test_cut_index_beyond_32_bit_digits_still_severs():
+    # tests/test_coupling.py:131-145: the banana preset with an external knife descending
+    # at 20 mm/s for 1.9 s, cut index 25: all three side values at that digit, two pieces
+    # of more than 30 % each.
+    from blademaster_gb300.presets import banana_config
+
+    cfg = replace(banana_config(), external_tool=True)
+    c = OracleSolver(cfg)
+    assert cut_capacity(c.node_count) >= 29
+    half, cut = cfg.blade_half_size[2], 25
+    for i in range(1900):
+        edge = max(0.0, 0.036 - 0.02 * i * 0.001)
+        state = ToolState([0.0, 0.0, edge + half], [0, 0, 0, 1], [0.0, 0.0, -0.02], [0, 0, 0])
+        c.external_interval(packed(state), round(0.001 / cfg.dt), cutting=True, cut_index=cut)
+    codes = c.get("codes")
+    assert set(np.unique(codes // 3**cut)) == {0, 1, 2}
+    _, sizes = components(c.node_numpy, c.weight_numpy, codes)
+    assert len(sizes) == 2 and sizes.min() > 0.3 * c.n
