@@ -14,7 +14,11 @@ bit-exactly with the oracle on the same inputs:
 * the cut-code capacity follows the grid size
   (tests/test_stress_replays.py:61-87);
 * a cut at index 25 (digit 3^25, beyond 32 bits) severs the banana into two
-  pieces (tests/test_coupling.py:131-145).
+  pieces (tests/test_coupling.py:131-145);
+* several free knives: only free knives may be several, slot order does not
+  matter, mirrored knives move alike and label their own digits, a knife
+  beside the block falls freely, each knife pays its own cutting work
+  (tests/test_multi_tool.py:21-106).
 """
 
 from dataclasses import replace
@@ -297,3 +301,97 @@ def test_cut_index_beyond_32_bit_digits_still_severs():
     assert set(np.unique(codes // 3**cut)) == {0, 1, 2}
     _, sizes = components(c.node_numpy, c.weight_numpy, codes)
     assert len(sizes) == 2 and sizes.min() > 0.3 * c.n
+
+
+# ------------------------------------------------------ several free knives
+
+def two_knives(**kwargs):
+    """tests/test_multi_tool.py:8-18"""
+    return OracleSolver(Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005, free_blade=True, tool_count=2,
+                               blade_half_size=(0.0005, 0.025, 0.02), **kwargs))
+
+
+def test_only_free_knives_may_be_several():
+    # test_multi_tool.py:21-26
+    for kwargs in ({}, {"pose_servo": True}, {"external_tool": True}):
+        with pytest.raises(ValueError):
+            Config(tool_count=2, **kwargs)
+    with pytest.raises(ValueError):
+        Config(tool_count=0)
+
+
+def dropped(xs, steps):
+    """test_multi_tool.py:29-36: two knives dropped at 0.6 m/s into the block."""
+    c = two_knives()
+    z = 0.03 + 0.02 + 0.002
+    c.set("tool_pos", [[x, 0.0, z] for x in xs])
+    c.set("tool_vel", [[0.0, 0.0, -0.6]] * 2)
+    for _ in range(steps):
+        c.step(cutting=True)
+    return c
+
+
+def test_knife_index_does_not_matter():
+    # test_multi_tool.py:39-44: swapping the knives' slots moves nothing beyond rounding
+    a, b = dropped([-0.015, 0.015], 100), dropped([0.015, -0.015], 100)
+    np.testing.assert_allclose(a.get("tool_pos"), b.get("tool_pos")[::-1], atol=1.0e-7)
+    np.testing.assert_allclose(a.get("x"), b.get("x"), atol=1.0e-6)
+
+
+def test_mirrored_knives_move_alike_and_label_their_own_digits():
+    # test_multi_tool.py:47-65 (60 steps keep the edges above the board)
+    steps = 60
+    c = dropped([-0.015, 0.015], steps)
+    p, v = c.get("tool_pos"), c.get("tool_vel")
+    np.testing.assert_allclose(p[0] * [-1, 1, 1], p[1], atol=1.0e-7)
+    np.testing.assert_allclose(v[0] * [-1, 1, 1], v[1], atol=1.0e-5)
+    assert 0.0 < p[0, 2] - 0.02 < 0.028
+    assert v[0, 2] > -0.6 - 9.81 * steps * 0.0005
+    codes = c.get("codes")
+    first, second = codes % 3, (codes // 3) % 3
+    assert set(np.unique(first)) == {0, 1, 2} and set(np.unique(second)) == {0, 1, 2}
+    assert np.all(codes < 9)
+    ref = c.reference
+    assert ref[first == 1, 0].max() < -0.015 < ref[first == 2, 0].min()
+    assert ref[second == 1, 0].max() < 0.015 < ref[second == 2, 0].min()
+
+
+def test_knife_beside_the_block_falls_freely():
+    # test_multi_tool.py:68-80
+    c = two_knives()
+    z0 = 0.2
+    c.set("tool_pos", [[-0.015, 0.0, 0.03 + 0.02 + 0.002], [0.2, 0.0, z0]])
+    n = 100
+    for _ in range(n):
+        c.step(cutting=True)
+    dt, g = 0.0005, 9.81
+    pos, vel = c.get("tool_pos"), c.get("tool_vel")
+    assert vel[1, 2] == pytest.approx(-g * n * dt, rel=1.0e-5)
+    assert pos[1, 2] == pytest.approx(z0 - g * dt * dt * n * (n + 1) / 2, abs=1.0e-6)
+    np.testing.assert_allclose(pos[1, :2], [0.2, 0.0], atol=1.0e-9)
+
+
+@pytest.mark.parametrize("first", [0, 1])
+def test_each_knife_pays_its_own_cutting_work(first):
+    # test_multi_tool.py:83-106: one particle under knife `first`, the others far away
+    c = two_knives(cutting_energy=1.0)
+    x = c.reference.copy()
+    x[:, 0] += 10
+    x[0] = [0, 0, 0.039]
+    c.set("x", x)
+    positions = np.array([[3.0, 0, 0.06], [3.0, 0, 0.06]])
+    positions[first, 0] = 0
+    c.set("tool_pos", positions)
+    c.set("tool_vel", [[0, 0, -1], [0, 0, -1]])
+    c.rigid_contacts(True)
+    initial = c.get("reaction")[first].copy()
+    assert c.get("tool_damage")[first][0] == 1
+    assert c.get("tool_damage")[1 - first][0] == 0
+    positions[:, 0] = positions[::-1, 0]
+    c.set("tool_pos", positions)
+    c.set("acc", 0)
+    c.rigid_contacts(True)
+    np.testing.assert_allclose(c.get("reaction")[1 - first], initial, rtol=1e-6)
+    assert c.get("tool_damage")[1 - first][0] == 1
+    c.set_cut(2)
+    assert not c.get("tool_damage").any()
