@@ -18,7 +18,10 @@ bit-exactly with the oracle on the same inputs:
 * several free knives: only free knives may be several, slot order does not
   matter, mirrored knives move alike and label their own digits, a knife
   beside the block falls freely, each knife pays its own cutting work
-  (tests/test_multi_tool.py:21-106).
+  (tests/test_multi_tool.py:21-106);
+* the paper's cutting resistance stops growing with the cutting energy,
+  while held particles make the force grow with it
+  (tests/test_cut_resistance.py:74-111).
 """
 
 from dataclasses import replace
@@ -395,3 +398,40 @@ def test_each_knife_pays_its_own_cutting_work(first):
     assert c.get("tool_damage")[1 - first][0] == 1
     c.set_cut(2)
     assert not c.get("tool_damage").any()
+
+
+# -------------------------------------------------------- cutting resistance
+
+RESIST_SIZE = (0.04, 0.02, 0.024)
+
+
+def steady_force(cutting_energy, **kwargs):
+    """Mean knife force while the edge is pushed from 4 to 12 mm depth at 50 mm/s
+    (test_cut_resistance.py:74-99), on the oracle."""
+    cfg = Config(size=RESIST_SIZE, grid_spacing=0.006, dt=0.0001, young_modulus=400000.0, poisson_ratio=0.4,
+                 yield_stress=40000.0, cutting_energy=cutting_energy, blade_half_size=(0.0005, 0.015, 0.02),
+                 external_tool=True, grid_storage="compact", **kwargs)
+    c = OracleSolver(cfg)
+    hz, speed, interval = cfg.blade_half_size[2], 0.05, 0.002
+    steps = round(interval / cfg.dt)
+    edges, forces = [], []
+    for i in range(int(0.016 / speed / interval)):
+        edge = RESIST_SIZE[2] + 0.002 - speed * i * interval
+        state = ToolState([0.0, 0.0, edge + hz], [0, 0, 0, 1], [0, 0, -speed], [0, 0, 0])
+        impulse, _, _ = c.external_interval(packed(state), steps, cutting=True, cut_index=0)
+        forces.append(float(impulse[2]) / interval)
+        edges.append(edge)
+    depth = RESIST_SIZE[2] - np.array(edges)
+    return np.mean(np.array(forces)[(depth > 0.004) & (depth < 0.012)])
+
+
+def test_paper_resistance_stops_growing_with_cutting_energy():
+    # test_cut_resistance.py:103-106: particles slide around the edge before their damage work is paid
+    low, high = steady_force(100.0), steady_force(1000.0)
+    assert high == pytest.approx(low, rel=0.05)
+
+
+def test_held_particles_make_the_force_grow_with_cutting_energy():
+    # test_cut_resistance.py:109-111
+    low, high = steady_force(100.0, cut_hold=True), steady_force(1000.0, cut_hold=True)
+    assert high > 3.0 * low > 0.0
