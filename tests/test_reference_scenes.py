@@ -21,7 +21,10 @@ bit-exactly with the oracle on the same inputs:
   (tests/test_multi_tool.py:21-106);
 * the paper's cutting resistance stops growing with the cutting energy,
   while held particles make the force grow with it
-  (tests/test_cut_resistance.py:74-111).
+  (tests/test_cut_resistance.py:74-111);
+* the single-field baseline: cut halves move independently, one field drags
+  the other half, switching back restores the separation
+  (tests/test_single_field.py:7-46).
 """
 
 from dataclasses import replace
@@ -435,3 +438,64 @@ def test_held_particles_make_the_force_grow_with_cutting_energy():
     # test_cut_resistance.py:109-111
     low, high = steady_force(100.0, cut_hold=True), steady_force(1000.0, cut_hold=True)
     assert high > 3.0 * low > 0.0
+
+
+# ------------------------------------------------------------- single field
+
+def set_single_field(c, enabled):
+    """Solver.set_single_field (solver.py:382-389) on the oracle: the transfers' codes switch
+    and the topology is marked dirty."""
+    from blademaster_gb300 import _native
+
+    if bool(enabled) != c.single_field:
+        c.single_field = bool(enabled)
+        c.arrays["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
+
+
+HALVES = Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005)
+
+
+def pushed_halves(single_field, steps=40):
+    """test_single_field.py:7-18: the left half (code 1) pushed at -0.2 m/s against the right (code 2)."""
+    c = OracleSolver(HALVES)
+    left = c.reference[:, 0] < 0
+    c.set("codes", np.where(left, 1, 2).astype(np.int64))
+    v = np.zeros((c.n, 3), np.float32)
+    v[left, 0] = -0.2
+    c.set("v", v)
+    set_single_field(c, single_field)
+    for _ in range(steps):
+        c.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
+    v = c.get("v")
+    return v[~left, 0].mean(), v[left, 0].mean(), c.get("codes")
+
+
+def test_cut_halves_move_independently():
+    # test_single_field.py:21-25
+    right, left, sides = pushed_halves(False)
+    assert abs(right) < 0.005
+    assert left < -0.1
+    assert set(np.unique(sides)) == {1, 2}
+
+
+def test_single_field_drags_the_other_half():
+    # test_single_field.py:28-31
+    right, _, sides = pushed_halves(True)
+    assert right < -0.05
+    assert set(np.unique(sides)) == {1, 2}
+
+
+def test_switching_back_restores_separation():
+    # test_single_field.py:34-46, with the cached topology rebuilt on the switch
+    c = OracleSolver(replace(HALVES, cache_topology=True))
+    left = c.reference[:, 0] < 0
+    c.set("codes", np.where(left, 1, 2).astype(np.int64))
+    set_single_field(c, True)
+    c.advance(np.tile([0.0, 0.0, 0.2], (4, 1)), cutting=False)
+    assert c.single_field
+    set_single_field(c, False)
+    v = np.zeros((c.n, 3), np.float32)
+    v[left, 0] = -0.2
+    c.set("v", v)
+    c.advance(np.tile([0.0, 0.0, 0.2], (40, 1)), cutting=False)
+    assert abs(c.get("v")[~left, 0].mean()) < 0.005
