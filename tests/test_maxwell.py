@@ -1,7 +1,9 @@
 """Maxwell (generalised standard linear solid) branch, material.py:478-618.
 
 CPU: the reference's held-deformation relaxation tests (tests/test_maxwell.py
-:85-106) on the oracle against the float64 closed form.  GPU: cut substeps
+:85-118) on the oracle against the float64 closed form, including a slow
+relaxation over 20000 steps, and a disabled branch (tau or fraction zero)
+reproducing the elastic run exactly (:21-32).  GPU: cut substeps
 with the Maxwell branch (and with plasticity on top) bit-exact against the
 oracle, including the float64 viscous state.
 """
