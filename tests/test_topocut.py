@@ -1,7 +1,8 @@
 """TopoCut topology discovery for the MLS baseline (topocut_topology.py:1-229).
 
 CPU: the oracle's cluster assignment on the reference's cube surface
-(tests/test_topocut_topology.py:66-143 of the reference).  GPU: the
+(tests/test_topocut_topology.py:66-143 of the reference), and the host
+smoothing and face components.  GPU: the
 reference's own behaviours (tests/test_topocut_topology.py:17-63), the
 device SDF against the brute-force oracle, the extracted surface closed and
 consistently oriented with the block's volume, and the device cluster
@@ -42,6 +43,31 @@ def test_oracle_deep_interior_assignment():
 
 # ------------------------------------------------------------------- GPU
 
+
+
+def test_host_smoothing_and_face_components():
+    # topocut_topology.py:81-114: Laplacian smoothing (Eq. 10) over the mesh edges, and the
+    # connected components of the faces through shared vertices
+    from blademaster_gb300.topocut import face_components, smooth
+
+    v = CUBE_VERTICES.astype(float)
+    smoothed = smooth(v, CUBE_FACES, 0.5, 3)
+    # a point-symmetric closed mesh keeps its centroid, and every vertex moves toward it
+    np.testing.assert_allclose(smoothed.mean(0), v.mean(0), atol=1e-12)
+    r0 = np.linalg.norm(v - v.mean(0), axis=1)
+    r = np.linalg.norm(smoothed - v.mean(0), axis=1)
+    assert np.all(r < r0)
+    np.testing.assert_array_equal(smooth(v, CUBE_FACES, 0.5, 0), v)
+    # one step equals v + alpha (mean of the edge neighbours - v)
+    one = smooth(v, CUBE_FACES, 0.5, 1)
+    k = 0
+    nbrs = {b for f in CUBE_FACES for a, b in zip(f, np.roll(f, 1)) if a == k} | \
+           {a for f in CUBE_FACES for a, b in zip(f, np.roll(f, 1)) if b == k}
+    np.testing.assert_allclose(one[k], v[k] + 0.5 * (v[sorted(nbrs)].mean(0) - v[k]), atol=1e-12)
+    # two disjoint cubes: two components, each cube's faces together
+    faces = np.concatenate([CUBE_FACES, CUBE_FACES + 8])
+    labels = face_components(faces, 16)
+    assert len(set(labels[:12])) == 1 and len(set(labels[12:])) == 1 and labels[0] != labels[12]
 
 
 @pytest.mark.gpu
