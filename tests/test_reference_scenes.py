@@ -499,3 +499,125 @@ def test_switching_back_restores_separation():
     c.set("v", v)
     c.advance(np.tile([0.0, 0.0, 0.2], (40, 1)), cutting=False)
     assert abs(c.get("v")[~left, 0].mean()) < 0.005
+
+
+# ------------------------------------------------------- CUDA twins of the above
+
+@pytest.mark.gpu
+def test_deep_digit_severs_on_cuda_and_matches_the_oracle_first():
+    # test_coupling.py:131-145 on the CUDA solver; its first 100 intervals bit-exact with the oracle
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.presets import banana_config
+    from blademaster_gb300.solver import Solver
+
+    cfg = replace(banana_config(), external_tool=True)
+    g, c = Solver(cfg), OracleSolver(cfg)
+    port = ExternalToolPort(g)
+    half, cut, steps = cfg.blade_half_size[2], 25, round(0.001 / cfg.dt)
+    for i in range(1900):
+        edge = max(0.0, 0.036 - 0.02 * i * 0.001)
+        state = ToolState([0.0, 0.0, edge + half], [0, 0, 0, 1], [0.0, 0.0, -0.02], [0, 0, 0])
+        port.advance(state, 0.001, cutting=True, cut_index=cut)
+        if i < 100:
+            c.external_interval(packed(state), steps, cutting=True, cut_index=cut)
+        if i == 99:
+            for name in ("x", "v", "codes", "damage"):
+                np.testing.assert_array_equal(getattr(g, name).numpy(), c.get(name), err_msg=name)
+    codes = g.codes.numpy()
+    assert set(np.unique(codes // 3**cut)) == {0, 1, 2}
+    _, sizes = g.components()
+    assert len(sizes) == 2 and sizes.min() > 0.3 * g.n
+
+
+def cuda_two_knives(**kwargs):
+    from blademaster_gb300.solver import Solver
+
+    return Solver(Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005, free_blade=True, tool_count=2,
+                         blade_half_size=(0.0005, 0.025, 0.02), **kwargs))
+
+
+@pytest.mark.gpu
+def test_several_knives_on_cuda_match_the_oracle():
+    # test_multi_tool.py:29-80 scenes, bit-exact with the oracle
+    z = 0.03 + 0.02 + 0.002
+    for xs, steps in (([-0.015, 0.015], 60), ([0.015, -0.015], 100)):
+        g, c = cuda_two_knives(), dropped(xs, steps)
+        g.tool_pos.assign([[x, 0.0, z] for x in xs])
+        g.tool_vel.assign([[0.0, 0.0, -0.6]] * 2)
+        for _ in range(steps):
+            g.step(cutting=True)
+        for name in ("x", "v", "codes"):
+            np.testing.assert_array_equal(getattr(g, name).numpy(), c.get(name), err_msg=name)
+        np.testing.assert_array_equal(g.tool_pos.numpy(), c.get("tool_pos").astype(np.float32))
+    g = cuda_two_knives()
+    g.tool_pos.assign([[-0.015, 0.0, z], [0.2, 0.0, 0.2]])
+    for _ in range(100):
+        g.step(cutting=True)
+    assert g.state()["blade_velocity"][1, 2] == pytest.approx(-9.81 * 100 * 0.0005, rel=1.0e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("first", [0, 1])
+def test_each_knife_pays_its_own_cutting_work_on_cuda(first):
+    # test_multi_tool.py:83-106 on the CUDA solver
+    g = cuda_two_knives(cutting_energy=1.0)
+    x = g.reference.copy()
+    x[:, 0] += 10
+    x[0] = [0, 0, 0.039]
+    g.x.assign(x)
+    positions = np.array([[3.0, 0, 0.06], [3.0, 0, 0.06]])
+    positions[first, 0] = 0
+    g.tool_pos.assign(positions)
+    g.tool_vel.assign([[0, 0, -1], [0, 0, -1]])
+    g.rigid_contacts(True)
+    initial = g.reaction.numpy()[first].copy()
+    assert g.tool_damage[first].numpy()[0] == 1 and g.tool_damage[1 - first].numpy()[0] == 0
+    positions[:, 0] = positions[::-1, 0]
+    g.tool_pos.assign(positions)
+    g.reaction.zero_()
+    g.torque.zero_()
+    g.rigid_contacts(True)
+    np.testing.assert_allclose(g.reaction.numpy()[1 - first], initial, rtol=1e-6)
+    assert g.tool_damage[1 - first].numpy()[0] == 1
+    g._set_cut(2)
+    assert all(not d.numpy().any() for d in g.tool_damage)
+
+
+@pytest.mark.gpu
+def test_single_field_halves_on_cuda_match_the_oracle():
+    # test_single_field.py:7-31 on the CUDA solver, bit-exact with the oracle after 40 substeps
+    from blademaster_gb300.solver import Solver
+
+    for single in (False, True):
+        g = Solver(HALVES)
+        left = g.reference[:, 0] < 0
+        g.codes.assign(np.where(left, 1, 2).astype(np.int64))
+        v = np.zeros((g.n, 3), np.float32)
+        v[left, 0] = -0.2
+        g.v.assign(v)
+        g.set_single_field(single)
+        for _ in range(40):
+            g.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
+        right_v, left_v, codes = pushed_halves(single)
+        np.testing.assert_array_equal(g.v.numpy()[~left, 0].mean(), right_v)
+        np.testing.assert_array_equal(g.codes.numpy(), codes)
+
+
+@pytest.mark.gpu
+def test_steady_cutting_force_on_cuda_matches_the_oracle():
+    # test_cut_resistance.py:74-111 scene on the CUDA solver: the same interval forces as the oracle
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.solver import Solver
+
+    for kwargs in ({}, {"cut_hold": True}):
+        cfg = Config(size=RESIST_SIZE, grid_spacing=0.006, dt=0.0001, young_modulus=400000.0, poisson_ratio=0.4,
+                     yield_stress=40000.0, cutting_energy=1000.0, blade_half_size=(0.0005, 0.015, 0.02),
+                     external_tool=True, grid_storage="compact", **kwargs)
+        g, c = Solver(cfg), OracleSolver(cfg)
+        port = ExternalToolPort(g)
+        for i in range(40):
+            edge = RESIST_SIZE[2] + 0.002 - 0.05 * i * 0.002
+            state = ToolState([0.0, 0.0, edge + 0.02], [0, 0, 0, 1], [0, 0, -0.05], [0, 0, 0])
+            r = port.advance(state, 0.002, cutting=True, cut_index=0)
+            impulse, _, _ = c.external_interval(packed(state), 20, cutting=True, cut_index=0)
+            np.testing.assert_array_equal(r.impulse_ns, impulse)
