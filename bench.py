@@ -8,12 +8,15 @@ edges starting 1 mm into the top face, moving down at 0.05 m/s; sorted-cell
 transfers and the skin-list pair search.  Synthetic inputs (the reference
 measures on no dataset).
 
-One step = one substep over every particle.  `value` times K substeps
-replayed as CUDA graphs with all state resident in HBM; `e2e` times the
-public API over the same substeps (Solver.advance, one batch of substeps per
-call) with the knife target copied from pinned host memory and the knife
-state read back every call; `e2e_single_substep` does the same with one
-substep per call.
+One step = one coupling interval of the workload (1 ms = 100 substeps for the
+block), replayed as one CUDA graph.  The warm-up steps run from t = 0; the
+solver is then restored to its t = 0 checkpoint, so the K timed steps are the
+scene's first K intervals (K = 20: the whole 2000-substep run of the block,
+with its settling, pair-list rebuilds and any re-registrations).  `value`
+times them with all state resident in HBM; `e2e` restores t = 0 again and
+times the same intervals through the public API (Solver.advance per interval)
+with the knife targets copied from pinned host memory and the knife state
+read back every call; `e2e_single_substep` does one substep per call.
 The CPU baseline runs the C oracle (the reference's algorithm restated, all
 host threads) on a bounded number of substeps of the same workload.
 
@@ -30,7 +33,6 @@ import subprocess
 import sys
 import tempfile
 import time
-from dataclasses import replace
 from pathlib import Path
 
 import numpy as np
@@ -45,43 +47,23 @@ UNIT = "particle-substeps/s"
 
 
 def workload(name):
-    from blademaster_gb300.solver import Config
+    """(Config, knife centres, knife velocities) of a scene workload (blademaster_gb300.scenes)."""
+    from blademaster_gb300 import scenes
 
     if name == "block_1p6M_8knives":
-        cfg = Config(
-            size=(0.20, 0.10, 0.08),
-            grid_spacing=0.002,
-            dt=1.0e-5,
-            density=1000.0,
-            young_modulus=2.0e5,
-            poisson_ratio=0.3,
-            free_blade=True,
-            tool_count=8,
-            blade_half_size=(0.0005, 0.06, 0.02),
-            cache_topology=True,
-        )
-        knives = np.array([[x, 0.0, 0.079 + 0.02] for x in np.arange(-0.07, 0.0701, 0.02)])
-        return cfg, knives, np.tile([0.0, 0.0, -0.05], (8, 1))
+        return scenes.block_8knives()
     if name == "block_3mm_8knives":
         # the same scene at 3 mm spacing (0.5 M particles, still larger than L2): profiling case
-        cfg, knives, velocity = workload("block_1p6M_8knives")
-        return replace(cfg, grid_spacing=0.003), knives, velocity
+        return scenes.block_8knives(spacing=0.003)
     if name == "freefall_8960":
-        cfg = Config(
-            size=(0.14, 0.10, 0.08),
-            grid_spacing=0.01,
-            dt=0.002,
-            density=1000.0,
-            young_modulus=2.0e5,
-            poisson_ratio=0.3,
-            free_blade=True,
-            blade_mass=0.2,
-            blade_half_size=(0.0005, 0.05, 0.02),
-            cache_topology=True,
-        )
-        return cfg, np.array([[0.0, 0.0, 0.08 + 0.005 + 0.02]]), np.zeros((1, 3))
+        # the gravity knife at the stable 0.25 ms step (the Table I step of 2 ms inverts the material)
+        return scenes.gravity_knife()
     raise ValueError(name)
 
+
+# Substeps of one bench step: one coupling interval of the workload (1 ms for the block,
+# so that 20 steps are its whole 2000-substep run; 50 ms for the gravity knife, 20 steps = 1 s).
+SUBSTEPS_PER_STEP = {"block_1p6M_8knives": 100, "block_3mm_8knives": 100, "freefall_8960": 200}
 
 # Algorithmic bytes of each stage: per particle, per registered (node, code) slot.
 STAGE_BYTES = {
@@ -404,9 +386,10 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
-    ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--batch", type=int, default=50, help="substeps per CUDA graph")
+    ap.add_argument("--steps", type=int, default=20, help="timed steps (coupling intervals)")
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--substeps", type=int, default=0,
+                    help="substeps per step (default: the workload's coupling interval)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="block_1p6M_8knives")
     ap.add_argument("--e2e-steps", type=int, default=100)
@@ -422,7 +405,6 @@ def main():
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -432,7 +414,10 @@ def main():
     if args.workload == "learned_c5":
         run_learned(args, rank, world)
         return
+    run_scene(args)
 
+
+def run_scene(args):
     import torch
 
     from blademaster_gb300 import replicas
@@ -447,28 +432,20 @@ def main():
     s = Solver(cfg, device=f"cuda:{local}")
     s.tool_pos.assign(knives)
     s.tool_vel.assign(velocity)
-    batch = max(1, min(args.batch, args.steps))
-    zeros = np.zeros((batch, 3))
+    per_step = args.substeps or SUBSTEPS_PER_STEP.get(args.workload, 100)
+    zeros = np.zeros((per_step, 3))
+    start_of_run = s.checkpoint()  # t = 0: the timed steps and the end-to-end steps both start here
 
-    def run(steps):
-        done = 0
-        while done < steps:
-            k = min(batch, steps - done)
-            s.advance(zeros[:k], cutting=True, graph=not args.eager)
-            done += k
+    def run(steps, graph=True):
+        for _ in range(steps):
+            s.advance(zeros, cutting=True, graph=graph and not args.eager)
 
-    run(args.warmup)
+    run(args.warmup)  # graph capture and upload, first touch of every array
 
-    def graph_kernels(k):
-        """Kernel launches of one replay of the k-substep graph (its kernel nodes)."""
-        count = ctypes.c_int64()
-        _native.check(s._lib.bm_graph_kernel_count(s.prepare(zeros[:k], True, 0), ctypes.byref(count)))
-        return count.value
-
-    # graphs are captured outside the timed region; eager runs launch the same kernels
-    timed_launches = (args.steps // batch) * graph_kernels(batch)
-    if args.steps % batch:
-        timed_launches += graph_kernels(args.steps % batch)
+    count = ctypes.c_int64()
+    _native.check(s._lib.bm_graph_kernel_count(s.prepare(zeros, True, 0), ctypes.byref(count)))
+    timed_launches = args.steps * count.value  # eager runs launch the same kernels
+    s.restore(start_of_run)
     torch.cuda.synchronize()
     clock_file = tempfile.NamedTemporaryFile(suffix=".csv", delete=False).name
     sampler = sample_clocks(clock_file)
@@ -485,8 +462,12 @@ def main():
         sampler.terminate()
         sampler.wait()
     ms = replicas.max_over_ranks(dist, start.elapsed_time(end), torch.cuda.current_device())
+    substeps = args.steps * per_step
     slots = int(s._t["nfield"].sum().item())
     counters_after = s._t["flags"].cpu().numpy()
+    errors = s.errors.numpy().tolist()
+    final_tool = s._t["tool"].cpu().numpy()
+
     def delta(name):
         return int(counters_after[_native.FLAG[name]] - counters_before[_native.FLAG[name]])
 
@@ -496,10 +477,11 @@ def main():
         "registrations": delta("REGISTRATIONS"),
         "multi_field_nodes": int(counters_after[_native.FLAG["MULTI"]]),
         "mixed_cells": int(counters_after[_native.FLAG["MIXED_CELLS"]]),
+        "simulated_s": substeps * cfg.dt,
     }
-    value = world * s.n * args.steps / (ms / 1e3)
+    value = world * s.n * substeps / (ms / 1e3)
 
-    # per-stage device time (CUDA events around each stage, eager launches)
+    # per-stage device time (CUDA events around each stage, eager launches), after the timed run
     stage_ms = (ctypes.c_float * len(_native.STAGES))()
     a = s._step_args(args.profile_steps, True, 0, use_targets=0)
     s._sync_step()
@@ -517,20 +499,19 @@ def main():
         stage_rooflines[name] = {"achieved_gbs": round(rate, 1), "frac": round(rate / peak, 4),
                                  "traffic": traffic_per_launch(name, s.n, slots)}
     substep_bytes = SUBSTEP_BYTES[0] * s.n + SUBSTEP_BYTES[1] * slots
-    substep_rate = substep_bytes / (ms / args.steps * 1e-3) / 1e9
+    substep_rate = substep_bytes / (ms / substeps * 1e-3) / 1e9
 
-    # End to end through the public API, as a caller drives the solver: each
+    # End to end through the public API, as a caller drives the solver, over
+    # the same intervals from the same t = 0 state as the timed region: each
     # Solver.advance call copies its host targets in (targets and orientations,
-    # 28 B a substep) and replays the batch's graph, and the caller reads the
-    # FP64 knife state back to pinned host memory and synchronises.  The main
-    # number uses the bench's batch of substeps per call; one substep per call
-    # is reported beside it.
+    # 28 B a substep) and replays the interval's graph, and the caller reads
+    # the float64 knife state back to pinned host memory and synchronises.
     pinned_state = torch.zeros(s._t["tool"].shape, dtype=torch.float64).pin_memory()
 
     def end_to_end(per_call, calls):
         host_targets = np.zeros((per_call, 3))
         s.advance(host_targets, True, 0)  # the graph exists before the timing
-        pinned_state.copy_(s._t["tool"], non_blocking=True)
+        s.restore(start_of_run)
         torch.cuda.synchronize()
         begin = time.perf_counter()
         for _ in range(calls):
@@ -540,12 +521,10 @@ def main():
         seconds = replicas.max_over_ranks(dist, time.perf_counter() - begin, torch.cuda.current_device())
         return world * s.n * per_call * calls / seconds
 
-    # as many substeps as the device-timed region, so both see the same mix of pair-list rebuilds
-    e2e_calls = max(2, args.steps // batch)
-    e2e_value = end_to_end(batch, e2e_calls)
+    e2e_value = end_to_end(per_step, args.steps)
+    e2e_same = bool(np.array_equal(pinned_state.numpy(), final_tool))
     e2e_single = end_to_end(1, args.e2e_steps)
 
-    errors = s.errors.numpy().tolist()
     line = {
         "metric": METRIC,
         "value": value,
@@ -563,11 +542,16 @@ def main():
             "workload": args.workload,
             "particles": s.n,
             "registered_slots": slots,
-            "substeps_per_graph": batch,
-            "l2": "inputs larger than L2 (particle state > 400 MB per substep), no flush",
+            "substeps_per_step": per_step,
+            "dt_s": cfg.dt,
+            "step": f"one {per_step * cfg.dt * 1e3:g} ms interval ({per_step} substeps, one graph replay); the "
+                    "timed steps restart from the t = 0 checkpoint after the warm-up",
+            "l2": "inputs larger than L2 (particle state > 400 MB per substep), no flush"
+                  if s.n > 1_000_000 else "small scene: the particle state fits in L2",
             "parallelism": f"replicas x{world}",
         },
-        "gpu_launches": None,
+        "ms_per_substep": ms / substeps,
+        "gpu_launches": timed_launches,
         "stage_ms": {k: round(v, 5) for k, v in stages.items()},
         "roofline": {
             "kernel": SINGLE_KERNEL_STAGES[dominant],
@@ -586,17 +570,17 @@ def main():
         "e2e": {
             "value": e2e_value,
             "unit": UNIT,
-            "h2d_bytes_per_step": 28 * batch,
+            "h2d_bytes_per_step": 28 * per_step,
             "d2h_bytes_per_step": int(pinned_state.numel() * 8),
-            "substeps_per_step": batch,
-            "call": "Solver.advance(host targets) + knife state read back, per batch of substeps",
+            "substeps_per_step": per_step,
+            "call": "Solver.advance(host targets) per interval + knife state read back, same intervals from t = 0",
+            "same_final_knife_state": e2e_same,
         },
         "e2e_single_substep": {"value": e2e_single, "unit": UNIT, "h2d_bytes_per_step": 28,
                                "d2h_bytes_per_step": int(pinned_state.numel() * 8)},
         "device_errors": errors,
         "timed_region_events": events,
     }
-    line["gpu_launches"] = timed_launches
     clocks = summarize_clocks(clock_file, torch.cuda.current_device()) if sampler else None
     line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -19,7 +19,7 @@ CSRC = PACKAGE.parent / "csrc"
 HEADER = PACKAGE.parent.parent / "include" / "blademaster_gb300.h"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libbm_gb300.so"
-SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_observe.cu", "bm_embed.cu", "bm_topocut.cu"]
+SOURCES = ["bm_material.cu", "bm_contact.cu", "bm_tool.cu", "bm_hold.cu", "bm_mls.cu", "bm_mlp.cu", "bm_capi.cu", "bm_noalloc.cu", "bm_mathprobe.cu", "bm_observe.cu", "bm_embed.cu", "bm_topocut.cu"]
 DEPENDS = ["bm_scalar.h", "bm_device.cuh", "bm_internal.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
@@ -220,6 +220,9 @@ def _declare(lib):
         "bm_g2p_probe": ([vp, vp, vp, vp, vp, vp, i, f, f, vp], i),
         "bm_resist_cut_probe": ([vp, vp, vp, vp, vp, vp, vp, vp, f, f, vp, f, i, u64p, vp, i, vp], i),
         "bm_plastic_project": ([vp, vp, i, f, f, vp, vp], i),
+        "bm_math_probe_f": ([i, vp, i, vp, vp], i),
+        "bm_math_probe_d": ([i, vp, vp, i, vp, vp], i),
+        "bm_svd_probe": ([vp, i, vp, vp, vp, vp, vp], i),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

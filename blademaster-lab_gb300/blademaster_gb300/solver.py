@@ -865,6 +865,31 @@ class Solver:
             raise RuntimeError("Inverted material; run is invalid")
         return state
 
+    def checkpoint(self):
+        """A device-side copy of the whole solver state (no counterpart in the reference).
+
+        Unlike ``state()``, which returns the reference's host dictionary, this
+        keeps everything a later substep reads: particle and grid arrays, cut
+        fields, pair lists, friction-history tables, knife state, accumulators
+        and counters.  ``restore`` of it makes the following substeps repeat
+        the ones that followed the checkpoint bit for bit.
+        """
+        import torch
+
+        with torch.cuda.device(self.device):
+            arrays = {name: t.clone() for name, t in self._t.items()}
+        return {"arrays": arrays, "step_count": self.step_count, "device_step": self._device_step,
+                "cut_index": self.cut_index, "single_field": self.single_field}
+
+    def restore(self, checkpoint):
+        """Copy a ``checkpoint()`` back in place (addresses, and so captured graphs, stay valid)."""
+        for name, saved in checkpoint["arrays"].items():
+            self._t[name].copy_(saved)
+        self.step_count = checkpoint["step_count"]
+        self._device_step = checkpoint["device_step"]
+        self.cut_index = checkpoint["cut_index"]
+        self.field_codes = self.single_field_codes if checkpoint["single_field"] else self.codes
+
     def synchronize(self):
         import torch
 

@@ -1,6 +1,7 @@
 """Mechanical pieces from the reference grid and the cut codes.
 
-Restates ``blademaster_warp/topology.py`` (compatible 6-14, components 17-57).
+Restates ``blademaster_warp/topology.py`` (compatible 6-14, components 17-57)
+with its own graph (particles joined through their fields, see components).
 A cut code is an integer in base 3, one digit per cut: 0 uncut, 1 / 2 the
 two sides.  Two codes are compatible unless some digit is non-zero in both
 and differs.  Pieces are connected components of the graph whose vertices
@@ -44,41 +45,51 @@ def digit_masks(codes):
 
 
 def components(nodes, weights, codes):
-    """Piece label of every particle and the piece sizes (topology.py:17-57)."""
+    """Piece label of every particle and the piece sizes (topology.py:17-57).
+
+    The same pieces as the device union-find (``Solver.components``), found
+    on the host: the (node, code) fields of the stencil nodes each particle
+    weighs are sorted, every particle joins the lowest-indexed particle of
+    each of its fields, and the lowest-indexed particles of two compatible
+    fields at one node join each other.  Pieces are the connected components
+    of that particle graph, numbered in the order of their lowest particle
+    index.
+    """
     from scipy.sparse import coo_matrix
     from scipy.sparse.csgraph import connected_components
 
     nodes = np.asarray(nodes)
-    weights = np.asarray(weights)
     codes = np.asarray(codes, np.int64)
     n = len(codes)
     if n == 0:
         return np.zeros(0, np.int64), np.zeros(0, np.int64)
-    used = weights > 0
-    owner = np.broadcast_to(np.arange(n)[:, None], nodes.shape)[used]
-    span = int(codes.max()) + 1
-    key = nodes[used].astype(np.int64) * span + codes[owner]
-    keys, vertex = np.unique(key, return_inverse=True)
-    key_node, key_code = keys // span, keys % span
-    rows, cols = [owner], [n + vertex.reshape(-1)]
-    distinct = np.unique(key_code)
-    ones, twos = digit_masks(distinct)
-    for i in range(len(distinct)):
-        for j in range(i + 1, len(distinct)):
-            if (ones[i] & twos[j]) == 0 and (twos[i] & ones[j]) == 0:
-                a = np.flatnonzero(key_code == distinct[i])
-                b = np.flatnonzero(key_code == distinct[j])
-                _, ia, ib = np.intersect1d(key_node[a], key_node[b], return_indices=True)
-                rows.append(n + a[ia])
-                cols.append(n + b[ib])
-    rows, cols = np.concatenate(rows), np.concatenate(cols)
-    size = n + len(keys)
-    graph = coo_matrix((np.ones(len(rows), np.int8), (rows, cols)), shape=(size, size))
-    _, label = connected_components(graph, directed=False)
-    label = label[:n]
-    first = np.full(label.max() + 1, n)
-    np.minimum.at(first, label, np.arange(n))
-    rank = np.empty_like(first)
-    rank[np.argsort(first, kind="stable")] = np.arange(len(first))
-    labels = rank[label]
+    particle, corner = np.nonzero(np.asarray(weights) > 0)
+    node = nodes[particle, corner].astype(np.int64)
+    code = codes[particle]
+    by_field = np.lexsort((particle, code, node))
+    node, code, particle = node[by_field], code[by_field], particle[by_field]
+    opens = np.ones(len(node), bool)
+    opens[1:] = (node[1:] != node[:-1]) | (code[1:] != code[:-1])
+    field = np.cumsum(opens) - 1
+    leader, field_node, field_code = particle[opens], node[opens], code[opens]
+    left, right = [particle], [leader[field]]
+    # fields of one node are adjacent: pair each with the ones d places on
+    first = np.flatnonzero(np.r_[True, field_node[1:] != field_node[:-1]])
+    count = np.diff(np.r_[first, len(field_node)])
+    end = np.repeat(first + count, count)
+    ones, twos = digit_masks(field_code)
+    index = np.arange(len(field_node))
+    for d in range(1, int(count.max())):
+        a = index[index + d < end]
+        b = a + d
+        joined = ((ones[a] & twos[b]) == 0) & ((twos[a] & ones[b]) == 0)
+        left.append(leader[a[joined]])
+        right.append(leader[b[joined]])
+    left, right = np.concatenate(left), np.concatenate(right)
+    graph = coo_matrix((np.ones(len(left), np.int8), (left, right)), shape=(n, n))
+    _, piece = connected_components(graph, directed=False)
+    _, lowest = np.unique(piece, return_index=True)  # lowest particle of each piece
+    number = np.empty(len(lowest), np.int64)
+    number[np.argsort(lowest)] = np.arange(len(lowest))
+    labels = number[piece]
     return labels, np.bincount(labels)

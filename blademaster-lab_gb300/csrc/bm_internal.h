@@ -89,7 +89,6 @@ void launch_tool_mirror(const bm_solver* s, cudaStream_t st);
 void launch_read_acc(const bm_solver* s, float* reaction, float* torque, float* board, float* work, cudaStream_t st);
 void launch_write_acc(const bm_solver* s, const float* reaction, const float* torque, const float* board,
                       const float* work, cudaStream_t st);
-void launch_step_counter(const bm_solver* s, cudaStream_t st);
 void launch_couple_probe(const int64_t* codes, const float* mass, const float* state, const int32_t* node_start,
                          int nodes, float* result, cudaStream_t st);
 void launch_g2p_probe(float* x, float* v, const int32_t* slots, const float* weights, const float* old_v,

@@ -794,11 +794,14 @@ __device__ void maxwell_at(const bm_params& P, const bm_buffers& B, int p, const
 }
 
 // material.maxwell_stress_at (material.py:536-566).
-__device__ void maxwell_stress_at(const bm_params& P, const bm_buffers& B, int p, float relax) {
+// material.maxwell_stress_at (material.py:536-566); with project == 0 the
+// stress of the current F, Fp and Fv alone (compute_stress_maxwell,
+// material.py:569-589: no return map, relax must be 0).
+__device__ void maxwell_stress_at(const bm_params& P, const bm_buffers& B, int p, float relax, int project = 1) {
     const int N = P.n;
     bm_m33 U, V;
     bm_v3 sigma;
-    if (P.yield_stress > 0.0f) {
+    if (project && P.yield_stress > 0.0f) {
         if (!plastic_at(P, B, p, P.yield_stress, &U, &sigma, &V)) {
             st9(B.stress, N, p, m33_zero());
             return;
@@ -836,7 +839,7 @@ __device__ void constitutive(const bm_params& P, const bm_buffers& B, int p) {
 __global__ void k_refresh_stress(bm_params P, bm_buffers B) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    if (P.maxwell) maxwell_stress_at(P, B, p, 0.0f);
+    if (P.maxwell) maxwell_stress_at(P, B, p, 0.0f, 0);
     else stress_at(P, B, p);
 }
 

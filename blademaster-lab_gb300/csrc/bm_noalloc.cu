@@ -30,7 +30,10 @@ int32_t* g_partials[kMaxDevices] = {};
 // Device address of g_scan_partials on the current device.  The first call on
 // each device makes the one runtime query (cudaGetSymbolAddress, which may
 // load this library's device code on that device); later calls read the
-// cached pointer.
+// cached pointer.  The cache is never invalidated: it assumes the device's
+// primary context lives as long as the process, so a cudaDeviceReset (after
+// which the module may load at another address) ends this entry point's use
+// in that process.
 int static_partials(int32_t** out) {
     int device = -1;
     if (cudaGetDevice(&device) != cudaSuccess) return bm::check_cuda("particle_contacts_static: current device");

@@ -68,17 +68,98 @@ __device__ bm_v3d vertex(int i, const bm_params& P) {
     return v3d(x, y, z);
 }
 
-// tool.inv_inertia (tool.py:141-143).
+// ----------------------------------------------------- warp-parallel step
+//
+// Float64 instructions issue slowly on this part (a warp instruction costs
+// the same whether one lane or 32 are active), so one warp runs each knife and
+// spreads the float64 work over its lanes.  Lane c (mod 3 for vectors, mod 4
+// for quaternions) evaluates component c of a vector expression with exactly
+// the operations of the one-thread form in bm_scalar.h, the operands picked
+// without a branch; shuffles then give every lane the whole vector.  Results
+// are therefore bit-identical to evaluating the expressions on one thread.
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ double pick3(bm_v3d a, int c) { return c == 0 ? a.x : (c == 1 ? a.y : a.z); }
+__device__ __forceinline__ double pick4(bm_qd q, int c) { return c == 0 ? q.x : (c == 1 ? q.y : (c == 2 ? q.z : q.w)); }
+__device__ __forceinline__ bm_v3d gather3(double mine) {
+    return v3d(__shfl_sync(kFull, mine, 0), __shfl_sync(kFull, mine, 1), __shfl_sync(kFull, mine, 2));
+}
+__device__ __forceinline__ bm_qd gather4(double mine) {
+    return qd(__shfl_sync(kFull, mine, 0), __shfl_sync(kFull, mine, 1), __shfl_sync(kFull, mine, 2),
+              __shfl_sync(kFull, mine, 3));
+}
+// Component c of v3d_cross(a, b).
+__device__ __forceinline__ double cross_c(bm_v3d a, bm_v3d b, int c) {
+    const int i = c == 2 ? 0 : c + 1, j = c == 0 ? 2 : c - 1;
+    return pick3(a, i) * pick3(b, j) - pick3(a, j) * pick3(b, i);
+}
+// Component c of qd_rotate(q, v) and qd_rotate_inv(q, v).
+__device__ __forceinline__ double rot_c(bm_qd q, bm_v3d v, int c) {
+    const bm_v3d u = v3d(q.x, q.y, q.z);
+    const double cc = 2.0 * q.w * q.w - 1.0;
+    const double d = 2.0 * v3d_dot(u, v);
+    return (pick3(v, c) * cc + pick3(u, c) * d) + cross_c(u, v, c) * (2.0 * q.w);
+}
+__device__ __forceinline__ double rot_inv_c(bm_qd q, bm_v3d v, int c) {
+    const bm_v3d u = v3d(q.x, q.y, q.z);
+    const double cc = 2.0 * q.w * q.w - 1.0;
+    const double d = 2.0 * v3d_dot(u, v);
+    return (pick3(v, c) * cc - cross_c(u, v, c) * (2.0 * q.w)) + pick3(u, c) * d;
+}
+// Component c (0..3) of qd_mul(a, b): both forms are evaluated, then selected.
+__device__ __forceinline__ double qmul_c(bm_qd a, bm_qd b, int c) {
+    const int i = c < 3 ? c : 0;
+    const double vec = a.w * pick4(b, i) + b.w * pick4(a, i) + cross_c(v3d(a.x, a.y, a.z), v3d(b.x, b.y, b.z), i);
+    const double scalar = a.w * b.w - ((a.x * b.x + a.y * b.y) + a.z * b.z);
+    return c < 3 ? vec : scalar;
+}
+// qd_normalize across lanes 0..3.
+__device__ __forceinline__ bm_qd normalize_warp(bm_qd q, int c) {
+    const double l = sqrt(((q.x * q.x + q.y * q.y) + q.z * q.z) + q.w * q.w);
+    if (l > 0.0) return gather4(pick4(q, c) / l);
+    return qd(0.0, 0.0, 0.0, 0.0);
+}
+
+// tool.inv_inertia (tool.py:141-143): one thread, and across lanes 0..2.
 __device__ __forceinline__ bm_v3d inv_inertia(bm_qd q, bm_v3d ii, bm_v3d torque) {
     return qd_rotate(q, v3d_cw(ii, qd_rotate_inv(q, torque)));
 }
+__device__ __forceinline__ bm_v3d inv_inertia_warp(bm_qd q, bm_v3d ii, bm_v3d torque, int c) {
+    const bm_v3d local = gather3(rot_inv_c(q, torque, c));
+    const bm_v3d scaled = gather3(pick3(ii, c) * pick3(local, c));
+    return gather3(rot_c(q, scaled, c));
+}
 
-// tool.step (tool.py:146-259) for knife k.
-__device__ void drive_one(const bm_params& P, const bm_buffers& B, int k, int index) {
+// True when no vertex of the knife can meet the board during this substep's
+// sweeps, shown in float32 with a margin: every vertex lies within R of the
+// centre, so its gap is at least x.z - R and its normal speed at least
+// -(|v.z| + |w| R); once the clearance exceeds twice dt times that speed,
+// desired = -gap/dt stays below the vertex's normal speed and no sweep
+// applies an impulse, so v and w pass through unchanged.  NaN never clears.
+__device__ __forceinline__ bool board_clear(const bm_params& P, bm_v3d x, bm_v3d v, bm_v3d w) {
+    const float reach = blade_radius(P) * 1.001f + 1.0e-6f;
+    const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
+    const float spin = sqrtf((wx * wx + wy * wy) + wz * wz) * 1.001f;
+    const float clearance = (float)x.z - reach;
+    const float travel = (float)P.dt_d * (fabsf((float)v.z) + spin * reach);
+    return clearance > 0.0f && clearance > 2.0f * travel + 1.0e-30f;
+}
+
+// tool.step (tool.py:146-259) for knife k, run by all 32 lanes of one warp;
+// lane 0 stores the result.
+__device__ void drive_warp(const bm_params& P, const bm_buffers& B, int k, int index) {
+    const int lane = threadIdx.x & 31, c = lane % 3, c4 = lane & 3;
     double* t = B.tool + 13 * k;
-    bm_v3d x = dget3(t), v = dget3(t + 3), w = dget3(t + 10);
-    bm_qd q = qd_normalize(qd(t[6], t[7], t[8], t[9]));
-    const bm_v3d reaction = acc_read3(B.acc, BM_ACC_REACTION(k)), torque = acc_read3(B.acc, BM_ACC_TORQUE(k));
+    const bm_v3d x = dget3(t);
+    bm_v3d v = dget3(t + 3), w = dget3(t + 10);
+    const bm_qd q = normalize_warp(qd(t[6], t[7], t[8], t[9]), c4);
+    bm_fx fr, ft;
+    fr.lo = B.acc[BM_ACC_REACTION(k) + 2 * c];
+    fr.hi = B.acc[BM_ACC_REACTION(k) + 2 * c + 1];
+    ft.lo = B.acc[BM_ACC_TORQUE(k) + 2 * c];
+    ft.hi = B.acc[BM_ACC_TORQUE(k) + 2 * c + 1];
+    const bm_v3d reaction = gather3(bm_fx_to_double(fr)), torque = gather3(bm_fx_to_double(ft));
     const double mass = P.blade_mass_d, dt = P.dt_d;
     bm_v3d force = v3d(0.0, 0.0, -9.81 * mass), servo_torque = v3d(0.0, 0.0, 0.0);
     if (P.free_blade == 0) {
@@ -97,65 +178,87 @@ __device__ void drive_one(const bm_params& P, const bm_buffers& B, int k, int in
         if (s > 1.0e-8) error = v3d_mul(vector, 2.0 * bm_atan2(s, dq.w) / s);
         servo_torque = v3d_sub(v3d_mul(error, P.rot_stiffness), v3d_mul(w, P.rot_damping));
     }
-    v = v3d_add(v, v3d_div(v3d_add(v3d_mul(force, dt), reaction), mass));
+    v = gather3(pick3(v, c) + (pick3(force, c) * dt + pick3(reaction, c)) / mass);
     bm_v3d ii = v3d(P.inertia_inv_d[0], P.inertia_inv_d[1], P.inertia_inv_d[2]);
     if (P.lock_rotation) {
         ii = v3d(0.0, 0.0, 0.0);
         w = v3d(0.0, 0.0, 0.0);
     } else {
-        const bm_v3d local_w = qd_rotate_inv(q, w);
-        const bm_v3d inertia = v3d(1.0 / ii.x, 1.0 / ii.y, 1.0 / ii.z);
-        const bm_v3d gyroscopic = qd_rotate(q, v3d_cross(local_w, v3d_cw(inertia, local_w)));
-        w = v3d_add(w, inv_inertia(q, ii, v3d_add(torque, v3d_mul(v3d_sub(servo_torque, gyroscopic), dt))));
+        const bm_v3d local_w = gather3(rot_inv_c(q, w, c));
+        const bm_v3d inertia = gather3(1.0 / pick3(ii, c));
+        const bm_v3d spun = gather3(pick3(inertia, c) * pick3(local_w, c));
+        const bm_v3d gyroscopic = gather3(rot_c(q, gather3(cross_c(local_w, spun, c)), c));
+        const bm_v3d drive = gather3(pick3(torque, c) + (pick3(servo_torque, c) - pick3(gyroscopic, c)) * dt);
+        w = gather3(pick3(w, c) + pick3(inv_inertia_warp(q, ii, drive, c), c));
     }
     const bm_v3d normal = v3d(0.0, 0.0, 1.0);
     bm_v3d total = v3d(0.0, 0.0, 0.0);
-    bm_v3d rv[10];
-    for (int i = 0; i < 10; ++i) rv[i] = qd_rotate(q, vertex(i, P));
-    for (int sweep = 0; sweep < 6; ++sweep)
-        for (int i = 0; i < 10; ++i) {
-            const bm_v3d r = rv[i], corner = v3d_add(x, r);
-            if ((P.board_half_d[0] > 0.0 && fabs(corner.x) > P.board_half_d[0]) ||
-                (P.board_half_d[1] > 0.0 && fabs(corner.y) > P.board_half_d[1]))
-                continue;
-            const double gap = corner.z;
-            const double vn = v3d_dot(v3d_add(v, v3d_cross(w, r)), normal);
-            double desired = -gap / dt;
-            if (gap < 0.0) desired *= 0.2;
-            if (vn < desired) {
-                const bm_v3d rn = v3d_cross(r, normal);
-                const double effective = 1.0 / mass + v3d_dot(rn, inv_inertia(q, ii, rn));
-                const double jn = (desired - vn) / effective;
-                bm_v3d impulse = v3d_mul(normal, jn);
-                v = v3d_add(v, v3d_div(impulse, mass));
-                w = v3d_add(w, inv_inertia(q, ii, v3d_cross(r, impulse)));
-                bm_v3d vt = v3d_add(v, v3d_cross(w, r));
-                vt = v3d_sub(vt, v3d_mul(normal, v3d_dot(vt, normal)));
-                const double sp = v3d_len(vt);
-                if (sp > 1.0e-10) {
-                    const bm_v3d direction = v3d_div(v3d_neg(vt), sp), rtd = v3d_cross(r, direction);
-                    const double wt = 1.0 / mass + v3d_dot(rtd, inv_inertia(q, ii, rtd));
-                    const double jt = sp / wt < P.friction_dynamic_d * jn ? sp / wt : P.friction_dynamic_d * jn;
-                    const bm_v3d tangent = v3d_mul(direction, jt);
-                    impulse = v3d_add(impulse, tangent);
-                    v = v3d_add(v, v3d_div(tangent, mass));
-                    w = v3d_add(w, inv_inertia(q, ii, v3d_cross(r, tangent)));
+    if (!board_clear(P, x, v, w)) {
+        // Sweep invariants of vertex `lane` (lanes 10..31 repeat vertex lane % 10).
+        const int me = lane % 10;
+        const bm_v3d r = qd_rotate(q, vertex(me, P)), corner = v3d_add(x, r);
+        const bool skip = (P.board_half_d[0] > 0.0 && fabs(corner.x) > P.board_half_d[0]) ||
+                          (P.board_half_d[1] > 0.0 && fabs(corner.y) > P.board_half_d[1]);
+        const double gap = corner.z;
+        double desired = -gap / dt;
+        if (gap < 0.0) desired *= 0.2;
+        const bm_v3d rn = v3d_cross(r, normal);
+        const double effective = 1.0 / mass + v3d_dot(rn, inv_inertia(q, ii, rn));
+        // Until a vertex acts, v and w stay as they are: when none acts on the
+        // first sweep's values, no sweep acts at all.
+        const double vn0 = v3d_dot(v3d_add(v, v3d_cross(w, r)), normal);
+        const unsigned acting = __ballot_sync(kFull, lane < 10 && !skip && vn0 < desired);
+        if (acting != 0u) {
+            for (int sweep = 0; sweep < 6; ++sweep)
+                for (int i = 0; i < 10; ++i) {
+                    if (__shfl_sync(kFull, (int)skip, i)) continue;
+                    const bm_v3d ri = v3d(__shfl_sync(kFull, r.x, i), __shfl_sync(kFull, r.y, i),
+                                          __shfl_sync(kFull, r.z, i));
+                    const double want = __shfl_sync(kFull, desired, i);
+                    const double vn = v3d_dot(v3d_add(v, v3d_cross(w, ri)), normal);
+                    if (vn < want) {
+                        const double jn = (want - vn) / __shfl_sync(kFull, effective, i);
+                        bm_v3d impulse = v3d_mul(normal, jn);
+                        v = v3d_add(v, v3d_div(impulse, mass));
+                        w = v3d_add(w, inv_inertia(q, ii, v3d_cross(ri, impulse)));
+                        bm_v3d vt = v3d_add(v, v3d_cross(w, ri));
+                        vt = v3d_sub(vt, v3d_mul(normal, v3d_dot(vt, normal)));
+                        const double sp = v3d_len(vt);
+                        if (sp > 1.0e-10) {
+                            const bm_v3d direction = v3d_div(v3d_neg(vt), sp), rtd = v3d_cross(ri, direction);
+                            const double wt = 1.0 / mass + v3d_dot(rtd, inv_inertia(q, ii, rtd));
+                            const double jt = sp / wt < P.friction_dynamic_d * jn ? sp / wt : P.friction_dynamic_d * jn;
+                            const bm_v3d tangent = v3d_mul(direction, jt);
+                            impulse = v3d_add(impulse, tangent);
+                            v = v3d_add(v, v3d_div(tangent, mass));
+                            w = v3d_add(w, inv_inertia(q, ii, v3d_cross(ri, tangent)));
+                        }
+                        total = v3d_add(total, impulse);
+                    }
                 }
-                total = v3d_add(total, impulse);
-            }
         }
-    x = v3d_add(x, v3d_mul(v, dt));
+    }
+    const bm_v3d xn = gather3(pick3(x, c) + pick3(v, c) * dt);
     const double speed = v3d_len(w);
-    if (speed > 1.0e-10) q = qd_normalize(qd_mul(qd_from_axis_angle(v3d_div(w, speed), dt * speed), q));
-    dput3(t, x);
-    dput3(t + 3, v);
-    t[6] = q.x;
-    t[7] = q.y;
-    t[8] = q.z;
-    t[9] = q.w;
-    dput3(t + 10, w);
-    dput3(B.table_impulse + 3 * k, total);
-    write_mirror(P, B, k);
+    bm_qd qn = q;
+    if (speed > 1.0e-10) {
+        const bm_v3d axis = gather3(pick3(w, c) / speed);
+        double s, co;
+        bm_sincos(0.5 * (dt * speed), &s, &co);
+        const bm_qd turn = qd(axis.x * s, axis.y * s, axis.z * s, co);
+        qn = normalize_warp(gather4(qmul_c(turn, q, c4)), c4);
+    }
+    if (lane == 0) {
+        dput3(t, xn);
+        dput3(t + 3, v);
+        t[6] = qn.x;
+        t[7] = qn.y;
+        t[8] = qn.z;
+        t[9] = qn.w;
+        dput3(t + 10, w);
+        dput3(B.table_impulse + 3 * k, total);
+        write_mirror(P, B, k);
+    }
 }
 
 // tool.accumulate_reaction (tool.py:6-16): interval sums about the world origin.
@@ -200,14 +303,10 @@ __device__ void finish_external(const bm_params& P, const bm_buffers& B) {
     B.speed[0] = 0.0f;
 }
 
-__global__ void k_tool(bm_params P, bm_buffers B, int mode, int index, int advance_step) {
+__global__ void k_tool(bm_params P, bm_buffers B, int mode) {
     const int k = threadIdx.x;
     if (mode == kToolFinishExternal) {
         if (k == 0) finish_external(P, B);
-    } else if (mode == kToolDrive || mode == kToolAccumulate) {
-        if (mode == kToolAccumulate && k == 0) accumulate_reaction(B);
-        __syncthreads();
-        if (k < P.tool_count) drive_one(P, B, k, index);
     } else if (mode == kToolClear) {
         if (k < P.tool_count) {
             acc_clear3(B.acc, BM_ACC_REACTION(k));
@@ -218,7 +317,17 @@ __global__ void k_tool(bm_params P, bm_buffers B, int mode, int index, int advan
             B.speed[0] = 0.0f;
         }
     }
-    (void)advance_step;
+}
+
+// One warp per knife (block k = knife k).  With accumulate, knife 0 first adds
+// the substep's reaction to the interval sums about its position at the start
+// of the substep (a single knife: the configuration refuses several).
+__global__ void __launch_bounds__(32) k_tool_drive(bm_params P, bm_buffers B, int accumulate, int index) {
+    if (accumulate && blockIdx.x == 0) {
+        if (threadIdx.x == 0) accumulate_reaction(B);
+        __syncwarp();
+    }
+    drive_warp(P, B, blockIdx.x, index);
 }
 
 // tool.load_external_state (tool.py:19-39).
@@ -361,10 +470,11 @@ __global__ void k_g2p_probe(float* x, float* v, const int32_t* slots, const floa
 // --------------------------------------------------------------- launches
 
 void launch_tool_step(const bm_solver* s, int mode, int target_index, int advance_step, cudaStream_t st) {
-    k_tool<<<1, 32, 0, st>>>(s->P, s->B, mode, target_index, advance_step);
-}
-void launch_step_counter(const bm_solver* s, cudaStream_t st) {
-    k_tool<<<1, 32, 0, st>>>(s->P, s->B, -1, 0, 1);
+    (void)advance_step;
+    if (mode == kToolDrive || mode == kToolAccumulate)
+        k_tool_drive<<<s->P.tool_count, 32, 0, st>>>(s->P, s->B, mode == kToolAccumulate, target_index);
+    else
+        k_tool<<<1, 32, 0, st>>>(s->P, s->B, mode);
 }
 void launch_load_external(const bm_solver* s, cudaStream_t st) { k_load_external<<<1, 1, 0, st>>>(s->P, s->B); }
 void launch_store_interval(const bm_solver* s, cudaStream_t st) { k_store_interval<<<1, 1, 0, st>>>(s->B); }

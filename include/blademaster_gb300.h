@@ -263,7 +263,10 @@ int bm_hold_constraint(bm_solver* s, void* stream);
  * fail.  Limit: pair-list tables of at most 1024 * BM_STATIC_SCAN_PARTIALS
  * buckets (bucket_mask + 1), else BM_ERR_ARGUMENT.  The first call on each
  * device (the current one) looks up the array's address and should come
- * before any stream capture.  Calls that overlap on one device (two streams,
+ * before any stream capture.  The address is kept for the life of the
+ * process: after cudaDeviceReset (or any teardown of the device's primary
+ * context) the library's device code may load elsewhere, so this entry point
+ * must not be called again in that process.  Calls that overlap on one device (two streams,
  * solvers or host threads) share the array and race: serialise them.
  * Results equal bm_particle_contacts'. */
 #define BM_STATIC_SCAN_PARTIALS 16384
@@ -434,6 +437,17 @@ int bm_resist_cut_probe(const float* j, const float* x, const float* v, const fl
                         float* result, int n, void* stream);
 /* material.plastic_project (material.py:434-442) on [9][n] F and Fp. */
 int bm_plastic_project(float* F, float* Fp, int n, float mu, float yield_stress, int32_t* errors, void* stream);
+/* Accuracy probes of the library's own arithmetic beside CUDA's.  No
+ * counterpart in the reference, which calls Warp's builtins (wp.log, wp.exp,
+ * wp.sin, wp.cos, wp.atan2, wp.svd3 at material.py:111,418,515,565,588 and
+ * tool.py:178-259); these measure the replacements.  bm_math_probe_f: kind
+ * 0 logf, 1 expf, 2 expm1f of x[i]; out[2i] = the library's, out[2i+1] =
+ * CUDA's.  bm_math_probe_d (float64): kind 0 sin, 1 cos of x[i], 2
+ * atan2(y[i], x[i]).  bm_svd_probe: row-major 3x3 matrices A[n] to
+ * U diag(sigma) V^T (the substep's SVD) and the polar rotation R. */
+int bm_math_probe_f(int kind, const float* x, int n, float* out, void* stream);
+int bm_math_probe_d(int kind, const double* x, const double* y, int n, double* out, void* stream);
+int bm_svd_probe(const float* A, int n, float* U, float* sigma, float* V, float* R, void* stream);
 
 /* ------------------------------------------------------------------------
  * MLS-MPM cutting baseline (blademaster_warp/mlsmpm.py): updated-Lagrangian

@@ -325,12 +325,14 @@ static void maxwell_at(const bm_params* P, orc_state* S, int64_t p, bm_m33 U, bm
     st9(S->stress, p, m33_add(equilibrium, m33_mul(kirchhoff, m33_transpose(m33_inverse(ld9(S->F, p))))));
 }
 
-/* material.maxwell_stress_at (material.py:536-566). */
-static void maxwell_stress_at(const bm_params* P, orc_state* S, int64_t p, float relax, int32_t* err) {
+/* material.maxwell_stress_at (material.py:536-566); with project == 0 the
+ * stress of the current F, Fp and Fv alone (compute_stress_maxwell,
+ * material.py:569-589: no return map, relax 0). */
+static void maxwell_stress_at(const bm_params* P, orc_state* S, int64_t p, float relax, int project, int32_t* err) {
     bm_m33 U, V, f;
     bm_v3 sigma;
     float J;
-    if (P->yield_stress > 0.0f) {
+    if (project && P->yield_stress > 0.0f) {
         if (!plastic_at(P, S, p, P->yield_stress, &U, &sigma, &V, err)) {
             st9(S->stress, p, m33_zero());
             return;
@@ -353,7 +355,7 @@ static void maxwell_stress_at(const bm_params* P, orc_state* S, int64_t p, float
 ORC_API void orc_refresh_stress(const bm_params* P, orc_state* S) {
     int64_t p;
     for (p = 0; p < P->n; ++p) {
-        if (P->maxwell) maxwell_stress_at(P, S, p, 0.0f, &S->errors[1]);
+        if (P->maxwell) maxwell_stress_at(P, S, p, 0.0f, 0, &S->errors[1]);
         else stress_at(P, S, p, &S->errors[1]);
     }
 }
@@ -365,7 +367,7 @@ ORC_API void orc_maxwell_hold(const bm_params* P, orc_state* S, int steps) {
     int64_t p;
     int k;
     for (k = 0; k < steps; ++k)
-        for (p = 0; p < P->n; ++p) maxwell_stress_at(P, S, p, P->maxwell_relax, &S->errors[1]);
+        for (p = 0; p < P->n; ++p) maxwell_stress_at(P, S, p, P->maxwell_relax, 1, &S->errors[1]);
 }
 
 /* material.plastic_project (material.py:434-442). */
@@ -777,7 +779,7 @@ ORC_API void orc_material_step(const bm_params* P, orc_state* S, const int64_t* 
         for (p = 0; p < P->n; ++p) {
             update_F(P, S, p);
             if (P->maxwell) {
-                maxwell_stress_at(P, S, p, P->maxwell_relax, &errors1);
+                maxwell_stress_at(P, S, p, P->maxwell_relax, 1, &errors1);
             } else if (P->plastic) {
                 bm_m33 U, V;
                 bm_v3 sg;

@@ -3,8 +3,12 @@ bm_particle_contacts on the same inputs, both called through the C-ABI.
 
 The two entry points run the same kernels in the same order, so every output
 of the pass (impulses, partner lists, bucket table, pair table, counters) must
-be equal, bit for bit, on each of two calls in a row.  This file is collected
-last so it also runs after the other GPU tests have used the library.
+be equal, bit for bit, on each of two calls in a row.  The static entry point must also leave the
+solver's own scan partials untouched and allocate nothing (torch's allocator
+and the device's free memory unchanged by a call).  The largest table has
+2048 scan tiles, more than one chunk of the tile-sum scan.  This file is
+collected last so it also runs after the other GPU tests have used the
+library.
 """
 
 import ctypes
@@ -64,17 +68,32 @@ def contacts(solver, entry, step):
     _native.check(getattr(solver._lib, entry)(solver._handle, solver._stream))
 
 
-@pytest.mark.parametrize("mode", ["list", "hash"])
-@pytest.mark.parametrize("spacing", [0.0075, 0.0015])
-def test_static_scratch_matches_particle_contacts_on_two_calls(mode, spacing):
+SENTINEL = -123457
+
+
+@pytest.mark.parametrize("mode,spacing,tiles", [("list", 0.0075, 2), ("hash", 0.0075, 2), ("list", 0.0015, 256),
+                                                ("hash", 0.0015, 256), ("list", 0.0008, 2048)])
+def test_static_scratch_matches_particle_contacts_on_two_calls(mode, spacing, tiles):
+    import torch
+
     cfg = replace(Config(), grid_spacing=spacing, pair_search=mode)
     existing, static = scene(cfg, seed=5)
-    assert static.buckets >= 1024 * (2 if spacing > 0.005 else 256)
+    # 2048 tiles: more than one 1024-partial chunk per thread in the tile-sum scan
+    assert static.buckets == 1024 * tiles
+    # the solver's own scan partials (scratch words 64 .. 64 + tiles) must stay untouched
+    own = static._t["scratch"][64 : 64 + tiles]
+    own.fill_(SENTINEL)
     for step in range(2):
         contacts(existing, "bm_particle_contacts", step)
-        contacts(static, "bm_particle_contacts_static", step)
         existing.synchronize()
         static.synchronize()
+        allocated, free = torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0]
+        contacts(static, "bm_particle_contacts_static", step)
+        static.synchronize()
+        assert torch.cuda.memory_allocated() == allocated, f"call {step}"
+        if step == 1:  # the first call may load the library's device code on this device
+            assert torch.cuda.mem_get_info()[0] == free
+        assert bool((own == SENTINEL).all()), f"call {step} wrote the solver's own scan partials"
         np.testing.assert_array_equal(static.impulses.numpy(), existing.impulses.numpy(), err_msg=f"call {step}")
         for name in COMPARED:
             np.testing.assert_array_equal(static._t[name].cpu().numpy(), existing._t[name].cpu().numpy(),
