@@ -308,6 +308,10 @@ class Solver:
         T["relist"] = zeros(n, dtype=i32)
         T["relist_list"] = zeros(n, dtype=i32)
         T["listed"] = zeros(n, dtype=i32)
+        T["reg_node_mark"] = zeros(self.node_count, dtype=i32)
+        T["reg_nodes"] = zeros(self.node_count, dtype=i32)
+        T["reg_cell_mark"] = zeros(int(np.prod(cells)), dtype=i32)
+        T["reg_cells"] = zeros(int(np.prod(cells)), dtype=i32)
         tool = np.zeros((K, 13))
         tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
         tool[:, 9] = 1.0
@@ -340,6 +344,7 @@ class Solver:
         self._params = self._make_params()
         T["scratch"] = zeros(int(self._lib.bm_scratch_words(ctypes.byref(self._params))), dtype=i32)
         T["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
+        T["flags"][_native.FLAG["HOST_DIRTY"]] = 1
         T["flags"][_native.FLAG["PAIR_DIRTY"]] = 1
         self._handle = None
         self._bind()
@@ -518,6 +523,10 @@ class Solver:
         def dirty_all():
             T["flags"][_native.FLAG["PAIR_DIRTY"]] = 1
             T["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
+            T["flags"][_native.FLAG["HOST_DIRTY"]] = 1
+
+        def dirty_topology():
+            T["flags"][_native.FLAG["HOST_DIRTY"]] = 1
 
         self.x = particle_view(T["x"], o, r, (3,), np.float32, "x", dirty_pairs)
         self.v = particle_view(T["v"], o, r, (3,), np.float32, "v", dirty_pairs)
@@ -549,7 +558,9 @@ class Solver:
         self.errors = plain_view(T["errors"], (3,), np.int32, "errors")
         self.speed = plain_view(T["speed"], (1,), np.float32, "speed")
         flags = T["flags"]
-        self.topology_dirty = plain_view(flags[_native.FLAG["TOPOLOGY_DIRTY"] : _native.FLAG["TOPOLOGY_DIRTY"] + 1], (1,), np.int32, "topology_dirty")
+        # a host write of the flag asks for a full registration (HOST_DIRTY); the device's side
+        # labelling sets it alone and registers only the nodes around the relabelled particles
+        self.topology_dirty = plain_view(flags[_native.FLAG["TOPOLOGY_DIRTY"] : _native.FLAG["TOPOLOGY_DIRTY"] + 1], (1,), np.int32, "topology_dirty", dirty_topology)
         self.pair_list_dirty = plain_view(flags[_native.FLAG["PAIR_DIRTY"] : _native.FLAG["PAIR_DIRTY"] + 1], (1,), np.int32, "pair_list_dirty")
         self.pair_list_builds = plain_view(flags[_native.FLAG["PAIR_BUILDS"] : _native.FLAG["PAIR_BUILDS"] + 1], (1,), np.int32, "pair_list_builds")
         self.pair_count = [plain_view(T["pair_count"][i : i + 1], (1,), np.int32, f"pair_count[{i}]") for i in range(2)]

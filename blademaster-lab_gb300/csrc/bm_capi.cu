@@ -198,7 +198,8 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
                               buffers->scratch, buffers->cell_part, buffers->cell_field, buffers->hist_mask,
                               buffers->changed, buffers->relist, buffers->relist_list, buffers->listed,
                               buffers->multi_nodes, buffers->mixed_cells,
-                              buffers->particle_key, buffers->bucket_key, buffers->bucket_pos};
+                              buffers->particle_key, buffers->bucket_key, buffers->bucket_pos,
+                              buffers->reg_node_mark, buffers->reg_nodes, buffers->reg_cell_mark, buffers->reg_cells};
     for (const void* ptr : required)
         if (!ptr) return fail(BM_ERR_ARGUMENT, "a required buffer is null");
     if (P.maxwell && !buffers->viscous) return fail(BM_ERR_ARGUMENT, "maxwell requires the viscous buffer");

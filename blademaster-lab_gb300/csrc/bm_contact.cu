@@ -470,11 +470,7 @@ __global__ void k_prologue(bm_params P, bm_buffers B, int clear_step, int regist
     }
     if (threadIdx.x == 0) {
         if (P.pair_search != 0 || B.flags[BM_FLAG_PAIR_DIRTY] != 0) B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f
-        if (registration == 1 || (registration == 0 && B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0)) {
-            B.flags[BM_FLAG_MULTI] = 0;
-            B.flags[BM_FLAG_MIXED_CELLS] = 0;
-            B.flags[BM_FLAG_REGISTRATIONS] += 1;
-        }
+        if (registration >= 0) begin_registration(B, registration);
     }
     __syncthreads();
     if (threadIdx.x == 0) B.pair_count[nw] = 0;
@@ -678,11 +674,74 @@ __device__ void build_list(const bm_params& P, const bm_buffers& B, int p, float
     }
 }
 
+// build_list for particle p by one warp: lane i < 27 scans neighbour cell i
+// of the build grid and adds the partners it finds to `found` (this warp's
+// shared-memory list); the list overflows past BM_PAIR_LANES partners as in
+// build_list, otherwise each lane ranks its entries into ascending order.
+// The result equals build_list's; a relist touches few particles, so the
+// 27 bucket walks run side by side instead of one after another.
+__device__ void build_list_warp(const bm_params& P, const bm_buffers& B, int p, float reach, int32_t* found,
+                                int* found_count) {
+    const int N = P.n, lane = threadIdx.x & 31;
+    const bm_v3 xp = ld3(B.built_x, N, p), rp = ld3(B.ref, N, p);
+    const int64_t cp = B.codes[p];
+    if (lane == 0) B.built_codes[p] = cp;
+    if (cp == 0) {
+        const float largest = __int_as_float(B.flags[BM_FLAG_MAX_DISP]);
+        if ((v3_len(v3_sub(xp, rp)) + largest) + reach < 0.999f * (2.0f * P.spacing)) {
+            if (lane == 0) B.partner_count[p] = 0;
+            return;
+        }
+    }
+    if (lane == 0) *found_count = 0;
+    __syncwarp();
+    if (lane < 27) {
+        const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
+        const int cx = hx + lane % 3 - 1, cy = hy + (lane / 3) % 3 - 1, cz = hz + lane / 9 - 1;
+        const int b = list_bucket(cx, cy, cz, P.bucket_mask);
+        const int64_t key = cell_key(cx, cy, cz);
+        const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
+        const int begin = B.bucket_start[b], end = B.bucket_start[b + 1];
+        for (int it = begin; it < end; ++it) {
+            if (B.bucket_key[it] != key) continue;
+            const int q = B.bucket_items[it];
+            if (q == p) continue;
+            const float4 xq4 = bpos[it];
+            if (!(v3_len(v3_sub(v3(xq4.x, xq4.y, xq4.z), xp)) < reach)) continue;
+            if (v3_len(v3_sub(rp, ld3(B.ref, N, q))) < 2.0f * P.spacing && compatible_codes(cp, B.codes[q])) continue;
+            const int at = atomicAdd(found_count, 1);
+            if (at < BM_PAIR_LANES) found[at] = q;
+        }
+    }
+    __syncwarp();
+    const int total = *found_count;
+    int count = total > BM_PAIR_LANES ? -1 : total;
+    if (count > 0) {
+        int32_t* list = B.partners + (int64_t)p * BM_PAIR_LANES;
+        for (int j = lane; j < count; j += 32) {
+            const int q = found[j];
+            int rank = 0;
+            for (int k = 0; k < count; ++k) rank += found[k] < q;
+            list[rank] = q;
+        }
+    }
+    if (lane == 0) {
+        B.partner_count[p] = count;
+        if (count != 0 && B.listed[p] == 0) {
+            B.listed[p] = 1;
+            const int at = atomicAdd(&B.flags[BM_FLAG_CANDIDATES], 1);
+            if (at < P.candidate_capacity) B.candidates[at] = p;
+        }
+    }
+    __syncwarp();  // `found` is reused by this warp's next particle
+}
+
 // Cut codes changed since the last list update: mark each changed particle
 // and every particle within the build reach of it (build positions and
 // buckets), so their lists are recomputed with the new codes.  Codes only
 // gain digits, so compatibility only turns false and lists only grow; the
 // positions are still within half a skin of the build (else a full build ran).
+// One warp per changed particle, lane i < 27 walking neighbour cell i.
 __global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in, int clear_dirty) {
     const int changed = min(B.flags[BM_FLAG_CHANGED], P.n);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -690,37 +749,41 @@ __global__ void k_relist_mark(bm_params P, bm_buffers B, const float* reach_in, 
         if (changed != 0) B.flags[BM_FLAG_RELISTS] += 1;
     }
     if (changed == 0) return;
-    const int N = P.n;
+    const int N = P.n, lane = threadIdx.x & 31;
     const float reach = *reach_in;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < changed; t += gridDim.x * blockDim.x) {
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < changed; t += warps) {
         const int p = B.changed[t];
         const bm_v3 xp = ld3(B.built_x, N, p);
-        const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
-        const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
-        if (atomicExch(&B.relist[p], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = p;
-        for (int i = 0; i < 27; ++i) {
-            const int cx = hx + i % 3 - 1, cy = hy + (i / 3) % 3 - 1, cz = hz + i / 9 - 1;
+        if (lane == 0 && atomicExch(&B.relist[p], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = p;
+        if (lane < 27) {
+            const int hx = cell_coord(xp.x, reach), hy = cell_coord(xp.y, reach), hz = cell_coord(xp.z, reach);
+            const int cx = hx + lane % 3 - 1, cy = hy + (lane / 3) % 3 - 1, cz = hz + lane / 9 - 1;
             const int b = list_bucket(cx, cy, cz, P.bucket_mask);
             const int64_t key = cell_key(cx, cy, cz);
+            const float4* bpos = reinterpret_cast<const float4*>(B.bucket_pos);
             for (int it = B.bucket_start[b]; it < B.bucket_start[b + 1]; ++it) {
                 if (B.bucket_key[it] != key) continue;
                 const int q = B.bucket_items[it];
                 const float4 xq4 = bpos[it];
-                const bm_v3 xq = v3(xq4.x, xq4.y, xq4.z);
-                if (!(v3_len(v3_sub(xq, xp)) < reach)) continue;
+                if (!(v3_len(v3_sub(v3(xq4.x, xq4.y, xq4.z), xp)) < reach)) continue;
                 if (atomicExch(&B.relist[q], 1) == 0) B.relist_list[atomicAdd(&B.flags[BM_FLAG_RELIST], 1)] = q;
             }
         }
     }
 }
 
-__global__ void k_relist(bm_params P, bm_buffers B, const float* reach_in) {
+__global__ void __launch_bounds__(256) k_relist(bm_params P, bm_buffers B, const float* reach_in) {
+    __shared__ int32_t found[8][BM_PAIR_LANES];
+    __shared__ int found_count[8];
     const int count = min(B.flags[BM_FLAG_RELIST], P.n);
     if (count == 0) return;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    const int w = threadIdx.x >> 5;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + w; t < count; t += warps) {
         const int p = B.relist_list[t];
-        build_list(P, B, p, *reach_in, B.built_x);
-        B.relist[p] = 0;
+        build_list_warp(P, B, p, *reach_in, found[w], &found_count[w]);
+        if ((threadIdx.x & 31) == 0) B.relist[p] = 0;
     }
 }
 

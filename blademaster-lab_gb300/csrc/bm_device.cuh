@@ -245,6 +245,24 @@ __device__ __forceinline__ bm_m33 corotated_svd(const bm_m33& U, bm_v3 s, const 
     return m33_mul(m33_mul(m33_mul(U, m33_diag(d)), m33_transpose(V)), m33_transpose(plastic_inverse));
 }
 
+// The registration this substep runs (flags[BM_FLAG_REG_MODE]): none while the
+// topology is clean; full when forced, after a host write (BM_FLAG_HOST_DIRTY,
+// also set at creation) or a registration requested through the C-ABI;
+// otherwise incremental over the nodes the side labelling listed.
+__device__ __forceinline__ void begin_registration(const bm_buffers& B, int force) {
+    const bool dirty = force || B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0;
+    const int mode = !dirty ? 0 : ((force || B.flags[BM_FLAG_HOST_DIRTY] != 0) ? 1 : 2);
+    B.flags[BM_FLAG_REG_MODE] = mode;
+    if (mode != 0) {
+        B.flags[BM_FLAG_MULTI] = 0;
+        B.flags[BM_FLAG_REGISTRATIONS] += 1;
+    }
+    if (mode == 1) {
+        B.flags[BM_FLAG_MIXED_CELLS] = 0;
+        B.flags[BM_FLAG_HOST_DIRTY] = 0;
+    }
+}
+
 inline unsigned grid_for(int64_t count, int block = kBlock) {
     int64_t g = (count + block - 1) / block;
     return (unsigned)(g < 1 ? 1 : g);

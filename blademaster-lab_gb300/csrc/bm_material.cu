@@ -21,23 +21,21 @@ namespace bm {
 
 // Solver._register_topology, node pass: the distinct codes among a node's
 // contributors in ascending order (material.register, material.py:50-66).
-__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n);
+// With list_multi the node joins the multi-field node list when it has
+// more than one field.
+__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n,
+                              bool list_multi = true);
 
-__global__ void k_register_begin(bm_buffers B, int force) {
-    if (force || B.flags[BM_FLAG_TOPOLOGY_DIRTY] != 0) {
-        B.flags[BM_FLAG_MULTI] = 0;
-        B.flags[BM_FLAG_MIXED_CELLS] = 0;
-        B.flags[BM_FLAG_REGISTRATIONS] += 1;
-    }
-}
+__global__ void k_register_begin(bm_buffers B, int force) { begin_registration(B, force); }
 
-__global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
-    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+__global__ void k_register_nodes(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
+    if (B.flags[BM_FLAG_REG_MODE] != 1) return;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P.active_nodes; t += gridDim.x * blockDim.x)
         register_node(P, B, field_codes, B.active[t]);
 }
 
-__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n) {
+__device__ void register_node(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int n,
+                              bool list_multi) {
     int nf = 0;
     int64_t prev = 0;
     bool have_prev = false;
@@ -67,18 +65,20 @@ __device__ void register_node(const bm_params& P, const bm_buffers& B, const int
         have_prev = true;
     }
     B.nfield[n] = nf;
-    if (nf > 1) B.multi_nodes[atomicAdd(&B.flags[BM_FLAG_MULTI], 1)] = n;
+    if (list_multi && nf > 1) B.multi_nodes[atomicAdd(&B.flags[BM_FLAG_MULTI], 1)] = n;
 }
 
 // Particle pass: the field index of the particle's code at each stencil node.
-__device__ void register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int p);
+__device__ uint64_t register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes,
+                                      int p);
 
-__global__ void k_register_particles(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes, int force) {
-    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+__global__ void k_register_particles(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
+    if (B.flags[BM_FLAG_REG_MODE] != 1) return;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) register_particle(P, B, field_codes, p);
 }
 
-__device__ void register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes, int p) {
+__device__ uint64_t register_particle(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes,
+                                      int p) {
     const int64_t code = field_codes[p];
     const int base = B.base_node[p];
     uint64_t fidx = 0u;
@@ -91,6 +91,7 @@ __device__ void register_particle(const bm_params& P, const bm_buffers& B, const
         fidx |= (uint64_t)f << (8 * a);
     }
     B.fidx[p] = fidx;
+    return fidx;
 }
 
 __global__ void k_clear_flag(bm_buffers B, int which) { B.flags[which] = 0; }
@@ -166,8 +167,8 @@ __device__ __forceinline__ int cell_base_node(const bm_params& P, int c) {
 
 // Registration, cell pass: corner flags of every occupied cell and the list of
 // cells with a mixed corner.  Thread (cell, slot); lane s decides corner s.
-__global__ void k_register_cells(bm_params P, bm_buffers B, int force) {
-    if (!force && B.flags[BM_FLAG_TOPOLOGY_DIRTY] == 0) return;
+__global__ void k_register_cells(bm_params P, bm_buffers B) {
+    if (B.flags[BM_FLAG_REG_MODE] != 1) return;
     const int cells = cell_count(P);
     const int stride = gridDim.x * blockDim.x;
     for (int t0 = blockIdx.x * blockDim.x; t0 < 8 * cells; t0 += stride) {
@@ -197,6 +198,84 @@ __global__ void k_register_cells(bm_params P, bm_buffers B, int force) {
         if (s == 0 && ((any >> group) & 0xffu)) B.mixed_cells[atomicAdd(&B.flags[BM_FLAG_MIXED_CELLS], 1)] = c;
     }
 }
+
+// Incremental registration (flags[BM_FLAG_REG_MODE] == 2).  The side labelling
+// lists the stencil nodes of every particle it relabels (reg_nodes); only
+// those nodes, the particles of the cells around them and those cells'
+// corner flags are registered again.  Every other node, particle and cell
+// keeps what it has, which equals a full registration's, because none of
+// their contributors' codes changed.  The multi-field node list is rebuilt
+// from the field counts (its order is immaterial: each node is summed alone).
+
+__global__ void k_register_nodes_listed(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
+    if (B.flags[BM_FLAG_REG_MODE] != 2) return;
+    const int count = min(B.flags[BM_FLAG_REG_NODES], P.node_count);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int n = B.reg_nodes[t];
+        register_node(P, B, field_codes, n, false);
+        for (int a = 0; a < 8; ++a) {
+            const int c = cell_at(P, n, a);
+            if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
+            if (atomicExch(&B.reg_cell_mark[c], 1) == 0) B.reg_cells[atomicAdd(&B.flags[BM_FLAG_REG_CELLS], 1)] = c;
+        }
+    }
+}
+
+// Field indices of the listed cells' particles, then the cells' corner flags
+// (as k_register_cells: the common field of a corner, or kMixed).
+__global__ void k_register_cells_listed(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
+    if (B.flags[BM_FLAG_REG_MODE] != 2) return;
+    const int count = min(B.flags[BM_FLAG_REG_CELLS], cell_count(P));
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const int c = B.reg_cells[t];
+        const int begin = B.cell_start[c], end = B.cell_start[c + 1];
+        int lo[8], hi[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            lo[a] = kMixed;
+            hi[a] = 0;
+        }
+        for (int p = begin; p < end; ++p) {
+            const uint64_t fidx = register_particle(P, B, field_codes, p);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const int f = field_of(fidx, a);
+                lo[a] = min(lo[a], f);
+                hi[a] = max(hi[a], f);
+            }
+        }
+        const int base = cell_base_node(P, c);
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+            B.cell_field[(base + node_offset(P, a)) * 8 + a] = (uint8_t)(lo[a] != hi[a] ? kMixed : lo[a]);
+    }
+}
+
+// After either registration: clear the marks of the listed nodes and cells;
+// after an incremental one, list the multi-field nodes again.
+__global__ void k_register_finish(bm_params P, bm_buffers B) {
+    const int mode = B.flags[BM_FLAG_REG_MODE];
+    if (mode == 0) return;
+    const int nodes = min(B.flags[BM_FLAG_REG_NODES], P.node_count);
+    const int cells = min(B.flags[BM_FLAG_REG_CELLS], cell_count(P));
+    const int scan = mode == 2 ? P.active_nodes : 0;
+    const int total = max(max(nodes, cells), scan);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        if (t < nodes) B.reg_node_mark[B.reg_nodes[t]] = 0;
+        if (t < cells) B.reg_cell_mark[B.reg_cells[t]] = 0;
+        if (t < scan) {
+            const int n = B.active[t];
+            if (B.nfield[n] > 1) B.multi_nodes[atomicAdd(&B.flags[BM_FLAG_MULTI], 1)] = n;
+        }
+    }
+}
+
+__global__ void k_register_reset(bm_buffers B) {
+    B.flags[BM_FLAG_REG_NODES] = 0;
+    B.flags[BM_FLAG_REG_CELLS] = 0;
+    B.flags[BM_FLAG_REG_MODE] = 0;
+}
+
 
 struct P2GContrib {
     float m;
@@ -907,6 +986,12 @@ __device__ void assign_sides(const bm_params& P, const bm_buffers& B, int p, int
         // the pair lists of p and its neighbours are recomputed before the next pair pass
         const int at = atomicAdd(&B.flags[BM_FLAG_CHANGED], 1);
         if (at < P.n) B.changed[at] = p;
+        // and the nodes it weighs are registered again at the next registration
+        const int base = B.base_node[p];
+        for (int a = 0; a < 8; ++a) {
+            const int n = base + node_offset(P, a);
+            if (atomicExch(&B.reg_node_mark[n], 1) == 0) B.reg_nodes[atomicAdd(&B.flags[BM_FLAG_REG_NODES], 1)] = n;
+        }
     }
 }
 
@@ -1089,9 +1174,15 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     const unsigned gc = grid_for(cells8) < wide ? grid_for(cells8) : wide;
     if (begin) k_register_begin<<<1, 1, 0, st>>>(s->B, force);
-    k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes, force);
-    k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes, force);
-    k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B, force);
+    // full registration (each kernel returns at once unless the mode is 1)
+    k_register_nodes<<<gn, kBlock, 0, st>>>(P, s->B, field_codes);
+    k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes);
+    k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B);
+    // incremental registration (mode 2): a few hundred nodes and cells at most per substep
+    k_register_nodes_listed<<<152, 128, 0, st>>>(P, s->B, field_codes);
+    k_register_cells_listed<<<152, 128, 0, st>>>(P, s->B, field_codes);
+    k_register_finish<<<gn, kBlock, 0, st>>>(P, s->B);
+    k_register_reset<<<1, 1, 0, st>>>(s->B);
 }
 
 // Runs launch(q) on aux beside the work queued on st after this call, or on st

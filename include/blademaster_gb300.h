@@ -153,6 +153,11 @@ typedef struct bm_buffers {
     int32_t* relist;     /* [n] 1 while a particle's partner list awaits recomputation */
     int32_t* relist_list;/* [n] those particles */
     int32_t* listed;     /* [n] 1 if the particle is in candidates */
+    /* incremental topology registration (codes changed by side labelling only) */
+    int32_t* reg_node_mark; /* [node_count] 1 while a node awaits registration; zero between substeps */
+    int32_t* reg_nodes;     /* [node_count] those nodes */
+    int32_t* reg_cell_mark; /* [cells] 1 while a cell's particles await new field indices; zero between substeps */
+    int32_t* reg_cells;     /* [cells] those cells */
     /* tool and scalar state */
     double* tool;        /* [tools][13]: pos 3, vel 3, rot xyzw 4, omega 3 */
     float* tool_f;       /* [tools][BM_TOOL_F_WORDS] float32 mirror read by particle kernels */
@@ -207,6 +212,11 @@ typedef struct bm_buffers {
 #define BM_FLAG_HOLD_RESIDUAL 15 /* float bits: largest final residual (m/s) of any constraint solve so far */
 #define BM_FLAG_HOLD_COUNT 16    /* held-blade constraint: contacts this substep */
 #define BM_FLAG_HOLD_NODES 17    /* held-blade constraint: grid nodes the contacts touch */
+#define BM_FLAG_REG_MODE 18      /* this substep's registration: 0 none, 1 full, 2 incremental */
+#define BM_FLAG_REG_CHANGED 19   /* entries of buffers.changed the incremental registration reads */
+#define BM_FLAG_REG_NODES 20     /* entries of buffers.reg_nodes */
+#define BM_FLAG_REG_CELLS 21     /* entries of buffers.reg_cells */
+#define BM_FLAG_HOST_DIRTY 22    /* 1 after a host write that needs a full registration */
 #define BM_FLAG_WORDS 24
 
 typedef struct bm_solver bm_solver;

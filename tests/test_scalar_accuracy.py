@@ -90,7 +90,8 @@ def test_logf_within_two_and_a_half_ulp():
     special = np.array([0.0, -1.0, np.inf, np.nan, 1.0, 1.0e-45], np.float32)
     ours, _ = probe_f(0, special)
     assert ours[0] == -np.inf and np.isnan(ours[1]) and ours[2] == np.inf and np.isnan(ours[3]) and ours[4] == 0.0
-    assert abs(ours[5] - np.log(1.0e-45)) < 1e-4 * abs(np.log(1.0e-45))  # subnormal input
+    tiny = float(np.float32(1.0e-45))  # the smallest subnormal, 2^-149
+    assert abs(ours[5] - np.log(tiny)) <= 2.5 * float(np.spacing(np.float32(-np.log(tiny))))  # subnormal input
 
 
 def test_expf_within_two_ulp():
