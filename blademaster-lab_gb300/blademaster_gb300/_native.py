@@ -152,7 +152,7 @@ FLAG = {
     for k in ("TOPOLOGY_DIRTY", "PAIR_DIRTY", "PAIR_BUILDS", "STEP", "CANDIDATES", "EMBEDDED", "SLOTS", "CHANGED",
               "RELIST", "MULTI", "RELISTS", "MIXED_CELLS", "REGISTRATIONS", "MAX_DISP", "HOLD_NEEDS",
               "HOLD_RESIDUAL", "HOLD_COUNT", "HOLD_NODES", "REG_MODE", "REG_CHANGED", "REG_NODES", "REG_CELLS",
-              "HOST_DIRTY", "WORDS")
+              "HOST_DIRTY", "PAIR_SPEED", "WORDS")
 }
 CUT_ON, CUT_ADVANCE, CUT_HOLD = 1, 2, 4
 STAGES = ["prologue", "rigid", "pairs", "register", "p2g", "g2p", "remap", "tool", "fupdate", "assign"]

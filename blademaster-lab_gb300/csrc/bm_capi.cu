@@ -100,6 +100,15 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
             bm::launch_register(s, field_codes, force_topology ? 1 : 0, s->side, 0);
             cudaEventRecord(s->register_join, s->side);
         }
+        // The pair lists (full build when dirty, relists of changed codes) read
+        // positions, velocities and codes, which the contact pass does not
+        // write: outside profiling they run on their own stream beside it.
+        if (overlap) {
+            cudaEventRecord(s->lists_fork, st);
+            cudaStreamWaitEvent(s->lists, s->lists_fork, 0);
+            bm::launch_pair_lists(s, s->scan_partials, 1, s->lists);
+            cudaEventRecord(s->lists_join, s->lists);
+        }
         t.mark(1, st);
         bm::launch_rigid(s, a->cut_bits, st);
         t.mark(2, st);
@@ -117,7 +126,9 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
             bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, s->side);
             cudaEventRecord(s->join, s->side);
         }
-        bm::launch_pairs(s, st);
+        if (overlap) cudaStreamWaitEvent(st, s->lists_join, 0);
+        else bm::launch_pair_lists(s, s->scan_partials, 1, st);
+        bm::launch_pair_impulses(s, st);
         t.mark(3, st);
         if (overlap) cudaStreamWaitEvent(st, s->register_join, 0);
         else bm::launch_register(s, field_codes, force_topology ? 1 : 0, st, 0);
@@ -215,11 +226,15 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     s->B = *buffers;
     s->buckets = (int64_t)P.bucket_mask + 1;
     layout_scratch(s);
-    s->side = s->aux = nullptr;
+    s->side = s->aux = s->lists = nullptr;
     s->fork = s->join = s->register_fork = s->register_join = s->aux_fork = s->aux_join = nullptr;
+    s->lists_fork = s->lists_join = nullptr;
     if (cudaMemset(s->B.scratch + 1, 0, 63 * sizeof(int32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->lists, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->lists_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->lists_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->aux_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->aux_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -227,9 +242,10 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
         cudaEventCreateWithFlags(&s->register_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->register_join, cudaEventDisableTiming) != cudaSuccess) {
         const int rc = check_cuda("solver streams");
-        for (cudaStream_t q : {s->side, s->aux})
+        for (cudaStream_t q : {s->side, s->aux, s->lists})
             if (q) cudaStreamDestroy(q);
-        for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join})
+        for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join,
+                              s->lists_fork, s->lists_join})
             if (e) cudaEventDestroy(e);
         delete s;
         return rc;
@@ -240,11 +256,12 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
 
 int bm_solver_destroy(bm_solver* s) {
     if (!s) return BM_OK;
-    for (cudaStream_t q : {s->side, s->aux}) {
+    for (cudaStream_t q : {s->side, s->aux, s->lists}) {
         cudaStreamSynchronize(q);
         cudaStreamDestroy(q);
     }
-    for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join})
+    for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join,
+                          s->lists_fork, s->lists_join})
         cudaEventDestroy(e);
     delete s;
     return BM_OK;

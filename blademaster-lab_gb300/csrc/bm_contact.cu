@@ -469,49 +469,77 @@ __global__ void k_prologue(bm_params P, bm_buffers B, int clear_step, int regist
         if (threadIdx.x == 0) B.speed[0] = 0.0f;
     }
     if (threadIdx.x == 0) {
-        if (P.pair_search != 0 || B.flags[BM_FLAG_PAIR_DIRTY] != 0) B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f
+        if (P.pair_search != 0 || B.flags[BM_FLAG_PAIR_DIRTY] != 0) {
+            B.flags[BM_FLAG_MAX_DISP] = 0;  // +0.0f
+            B.flags[BM_FLAG_PAIR_SPEED] = 0;
+        }
         if (registration >= 0) begin_registration(B, registration);
     }
     __syncthreads();
     if (threadIdx.x == 0) B.pair_count[nw] = 0;
 }
 
-// First kernel of a full pair-list build.  Block 0 does
-// contact.set_pair_reach (contact.py:748-761) for the list search, or the
-// hash search reach 2 radius + 2 dt speed (contact.py:684), and resets the
-// build's counters; every block zeroes bucket counts and raises the largest
-// displacement |x - ref| over all particles (the build's reference-distance
-// bound, see build_list; k_prologue reset it).
-__global__ void k_pair_begin(bm_params P, bm_buffers B, float* reach_out, int64_t buckets, const int32_t* gate_flag) {
+// First kernel of a full pair-list build.  Block 0 resets the build's
+// counters; every block zeroes bucket counts and raises, over all particles,
+// the largest displacement |x - ref| (the build's reference-distance bound,
+// see build_list; k_prologue reset it).  The reach uses the substep's largest
+// particle speed (rigid_and_speed's maximum, contact.py:497): inside a
+// substep (find_speed) it is found here from the same velocities the contact
+// pass reads, so that the build need not wait for that pass; a pair pass
+// called on its own takes the stored maximum (buffers.speed), as the
+// reference's particle_contacts does.
+__global__ void k_pair_begin(bm_params P, bm_buffers B, int64_t buckets, const int32_t* gate_flag, int find_speed) {
     if (gate_flag && *gate_flag == 0) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const float speed = B.speed[0];
-        float value;
-        if (P.pair_search == 0) {
-            value = 2.0f * P.radius + P.pair_skin;
-            if (P.dt * speed > 0.5f * P.pair_skin) value += 2.0f * P.dt * speed;
-        } else {
-            value = 2.0f * P.radius + 2.0f * speed * P.dt;
-        }
-        *reach_out = value;
         B.flags[BM_FLAG_CANDIDATES] = 0;
         B.flags[BM_FLAG_PAIR_BUILDS] += 1;
         B.flags[BM_FLAG_CHANGED] = 0;  // a full build uses the current codes
+        if (!find_speed) B.flags[BM_FLAG_PAIR_SPEED] = __float_as_int(B.speed[0]);
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < buckets; i += stride) B.bucket_fill[i] = 0;
     const int N = P.n;
     float d = 0.0f;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x)
-        d = fmaxf(d, v3_len(v3_sub(ld3(B.x, N, p), ld3(B.ref, N, p))));
+    const float inf = __int_as_float(0x7f800000);
+    for (int p0 = blockIdx.x * blockDim.x; p0 < N; p0 += gridDim.x * blockDim.x) {
+        const int p = p0 + threadIdx.x;
+        const bool active = p < N;
+        float speed = -inf;
+        if (active) {
+            d = fmaxf(d, v3_len(v3_sub(ld3(B.x, N, p), ld3(B.ref, N, p))));
+            if (find_speed) speed = v3_len(ld3(B.v, N, p));
+        }
+        if (find_speed) {  // block-uniform
+            // the same maximum as the contact pass's (a NaN speed wins there too);
+            // every lane takes part in both warp collectives
+            const float vmax = warp_max(speed);
+            const bool any = __any_sync(0xffffffffu, active);
+            if ((threadIdx.x & 31) == 0 && any)
+                atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_PAIR_SPEED]), vmax);
+        }
+    }
     for (int s = 16; s > 0; s >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, s));
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_MAX_DISP]), d);
 }
 
-__global__ void k_bin_count(bm_params P, bm_buffers B, const float* reach_in, const int32_t* gate_flag) {
+// contact.set_pair_reach (contact.py:748-761) for the list search, or the hash
+// search reach 2 radius + 2 dt speed (contact.py:684), from the speed
+// k_pair_begin found.  Every thread evaluates it; block 0 stores it for the
+// build's later kernels and the relists.
+__device__ __forceinline__ float pair_reach(const bm_params& P, float speed) {
+    if (P.pair_search == 0) {
+        float value = 2.0f * P.radius + P.pair_skin;
+        if (P.dt * speed > 0.5f * P.pair_skin) value += 2.0f * P.dt * speed;
+        return value;
+    }
+    return 2.0f * P.radius + 2.0f * speed * P.dt;
+}
+
+__global__ void k_bin_count(bm_params P, bm_buffers B, float* reach_out, const int32_t* gate_flag) {
     if (gate_flag && *gate_flag == 0) return;
     const int64_t N = P.n;
-    const float reach = *reach_in;
+    const float reach = pair_reach(P, __int_as_float(B.flags[BM_FLAG_PAIR_SPEED]));
+    if (blockIdx.x == 0 && threadIdx.x == 0) *reach_out = reach;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) {
         const bm_v3 x = ld3(B.x, N, p);
         const int cx = cell_coord(x.x, reach), cy = cell_coord(x.y, reach), cz = cell_coord(x.z, reach);
@@ -935,13 +963,17 @@ void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st) {
 void launch_pairs(const bm_solver* s, cudaStream_t st) { launch_pairs_using(s, s->scan_partials, st); }
 
 void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st) {
-    const int force = s->P.pair_search != 0;
-    launch_pair_build(s, partials, !force, st);
-    if (!force) launch_relist(s, 1, st);
+    launch_pair_lists(s, partials, 0, st);
     launch_pair_impulses(s, st);
 }
 
-void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, cudaStream_t st) {
+void launch_pair_lists(const bm_solver* s, int32_t* partials, int find_speed, cudaStream_t st) {
+    const int force = s->P.pair_search != 0;
+    launch_pair_build(s, partials, !force, find_speed, st);
+    if (!force) launch_relist(s, 1, st);
+}
+
+void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, int find_speed, cudaStream_t st) {
     const bm_params& P = s->P;
     const bm_buffers& B = s->B;
     const int32_t* gate = gated ? &B.flags[BM_FLAG_PAIR_DIRTY] : nullptr;
@@ -952,7 +984,7 @@ void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, cudaStr
     const unsigned gb = grid_for(buckets) < wide ? grid_for(buckets) : wide;
     const unsigned gn = grid_for(P.n) < wide ? grid_for(P.n) : wide;
     const unsigned gt = tiles < 152 ? (unsigned)tiles : 152;
-    k_pair_begin<<<gn > gb ? gn : gb, kBlock, 0, st>>>(P, B, reach, buckets, gate);
+    k_pair_begin<<<gn > gb ? gn : gb, kBlock, 0, st>>>(P, B, buckets, gate, find_speed);
     k_bin_count<<<gn, kBlock, 0, st>>>(P, B, reach, gate);
     k_scan_tiles<<<gt, 1024, 0, st>>>(B.bucket_fill, B.bucket_start, buckets, partials, B.bucket_start + buckets,
                                       scan_ticket(B), gate);

@@ -14,7 +14,8 @@ struct bm_solver {
     int64_t buckets;
     cudaStream_t side;       // registration and knife integration run here, beside the main chain
     cudaStream_t aux;        // the multi-field node passes run here, beside the single-field ones
-    cudaEvent_t fork, join, register_fork, register_join, aux_fork, aux_join;
+    cudaStream_t lists;      // the pair-list build and relists run here, beside the contact pass
+    cudaEvent_t fork, join, register_fork, register_join, aux_fork, aux_join, lists_fork, lists_join;
 };
 
 struct bm_graph {
@@ -55,7 +56,15 @@ void launch_pairs_using(const bm_solver* s, int32_t* partials, cudaStream_t st);
 // returns at once unless flags[BM_FLAG_PAIR_DIRTY] is set, when `gated`),
 // the incremental relist of particles near changed codes (clearing
 // flags[BM_FLAG_PAIR_DIRTY] too, when `clear_dirty`), and the pair impulses.
-void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, cudaStream_t st);
+// find_speed: the build finds the largest particle speed itself (inside a
+// substep, beside the contact pass) instead of reading buffers.speed.
+void launch_pair_build(const bm_solver* s, int32_t* partials, int gated, int find_speed, cudaStream_t st);
+// The pair lists of this substep: the full build (gated on a dirty list, or
+// always in hash mode) and the relist of changed codes.  With find_speed they
+// read positions, velocities, codes and the build state only, none of which
+// the contact pass writes, so they may run beside it; the pair impulses
+// follow both.
+void launch_pair_lists(const bm_solver* s, int32_t* partials, int find_speed, cudaStream_t st);
 void launch_relist(const bm_solver* s, int clear_dirty, cudaStream_t st);
 void launch_pair_impulses(const bm_solver* s, cudaStream_t st);
 void launch_count_embedded(const bm_solver* s, int reset, cudaStream_t st);

@@ -207,47 +207,119 @@ __global__ void k_register_cells(bm_params P, bm_buffers B) {
 // their contributors' codes changed.  The multi-field node list is rebuilt
 // from the field counts (its order is immaterial: each node is summed alone).
 
+// register_node for node n by one warp: lane l takes slots 2 (l & 3) and
+// 2 (l & 3) + 1 of the cell at corner l >> 2, so the node's contributions
+// load in one round trip; each field is then the smallest code above the
+// previous field's, found by a warp minimum.  Same fields as register_node.
+__device__ void register_node_warp(const bm_params& P, const bm_buffers& B, const int64_t* __restrict__ field_codes,
+                                   int n) {
+    const int lane = threadIdx.x & 31, a = lane >> 2;
+    const int64_t none = INT64_MAX;  // codes stay below 3^40 < 2^63
+    int64_t mine[2] = {none, none};
+    const int c = cell_at(P, n, a);
+    if (c >= 0) {
+        const int begin = B.cell_start[c], count = B.cell_start[c + 1] - begin;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int slot = 2 * (lane & 3) + k;
+            if (slot < count) mine[k] = field_codes[begin + slot];
+        }
+    }
+    int nf = 0;
+    int64_t prev = -1;  // codes are non-negative
+    for (;;) {
+        int64_t best = none;
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+            if (mine[k] > prev && mine[k] < best) best = mine[k];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            const int64_t other = __shfl_xor_sync(kFull, best, d);
+            best = other < best ? other : best;
+        }
+        if (best == none) break;
+        if (nf >= P.fmax) {
+            if (lane == 0) atomicAdd(&B.errors[0], 1);
+            break;
+        }
+        if (lane == 0) {
+            const int s = nf * P.node_count + n;
+            B.fcode[s] = best;
+            uint64_t ones, twos;
+            digit_masks(best, &ones, &twos);
+            B.fones[s] = ones;
+            B.ftwos[s] = twos;
+        }
+        ++nf;
+        prev = best;
+    }
+    if (lane == 0) B.nfield[n] = nf;
+}
+
 __global__ void k_register_nodes_listed(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
     if (B.flags[BM_FLAG_REG_MODE] != 2) return;
     const int count = min(B.flags[BM_FLAG_REG_NODES], P.node_count);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, warps = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < count; t += warps) {
         const int n = B.reg_nodes[t];
-        register_node(P, B, field_codes, n, false);
-        for (int a = 0; a < 8; ++a) {
-            const int c = cell_at(P, n, a);
-            if (c < 0 || B.cell_start[c + 1] == B.cell_start[c]) continue;
-            if (atomicExch(&B.reg_cell_mark[c], 1) == 0) B.reg_cells[atomicAdd(&B.flags[BM_FLAG_REG_CELLS], 1)] = c;
+        register_node_warp(P, B, field_codes, n);
+        if (lane < 8) {
+            const int c = cell_at(P, n, lane);
+            if (c >= 0 && B.cell_start[c + 1] != B.cell_start[c] && atomicExch(&B.reg_cell_mark[c], 1) == 0)
+                B.reg_cells[atomicAdd(&B.flags[BM_FLAG_REG_CELLS], 1)] = c;
         }
     }
 }
 
-// Field indices of the listed cells' particles, then the cells' corner flags
-// (as k_register_cells: the common field of a corner, or kMixed).
+// Field indices of a listed cell's particles, then the cell's corner flags
+// (as k_register_cells: the common field of a corner, or kMixed), by one
+// warp: lane l takes particle slot l >> 2 of the cell and its corners
+// 2 (l & 3) and 2 (l & 3) + 1.  A cell holds at most 8 particles.
 __global__ void k_register_cells_listed(bm_params P, bm_buffers B, const int64_t* __restrict__ field_codes) {
     if (B.flags[BM_FLAG_REG_MODE] != 2) return;
     const int count = min(B.flags[BM_FLAG_REG_CELLS], cell_count(P));
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, slot = lane >> 2, pair = lane & 3;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < count; t += warps) {
         const int c = B.reg_cells[t];
-        const int begin = B.cell_start[c], end = B.cell_start[c + 1];
-        int lo[8], hi[8];
+        const int begin = B.cell_start[c], cnt = B.cell_start[c + 1] - begin;
+        const bool present = slot < cnt;
+        const int p = begin + (present ? slot : 0);
+        const int64_t code = field_codes[p];
+        const int base = B.base_node[p];
+        int f[2];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            lo[a] = kMixed;
-            hi[a] = 0;
+        for (int k = 0; k < 2; ++k) {
+            const int node = base + node_offset(P, 2 * pair + k);
+            const int nf = B.nfield[node];
+            int i = 0;
+            while (i < nf && B.fcode[(int64_t)i * P.node_count + node] != code) ++i;
+            f[k] = i >= nf ? 0 : i;  // only after a field overflow, already counted in errors[0]
         }
-        for (int p = begin; p < end; ++p) {
-            const uint64_t fidx = register_particle(P, B, field_codes, p);
+        uint64_t part = ((uint64_t)f[0] << (16 * pair)) | ((uint64_t)f[1] << (16 * pair + 8));
+        part |= __shfl_xor_sync(kFull, part, 1);
+        part |= __shfl_xor_sync(kFull, part, 2);
+        if (present && pair == 0) B.fidx[p] = part;
+        // corner a = 2 pair + k over the present particles: lanes of equal pair, stride 4
+        int lo[2], hi[2];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) {
-                const int f = field_of(fidx, a);
-                lo[a] = min(lo[a], f);
-                hi[a] = max(hi[a], f);
+        for (int k = 0; k < 2; ++k) {
+            lo[k] = present ? f[k] : kMixed;
+            hi[k] = present ? f[k] : 0;
+#pragma unroll
+            for (int d = 4; d < 32; d <<= 1) {
+                lo[k] = min(lo[k], __shfl_xor_sync(kFull, lo[k], d));
+                hi[k] = max(hi[k], __shfl_xor_sync(kFull, hi[k], d));
             }
         }
-        const int base = cell_base_node(P, c);
+        if (slot == 0) {
+            const int cbase = cell_base_node(P, c);
 #pragma unroll
-        for (int a = 0; a < 8; ++a)
-            B.cell_field[(base + node_offset(P, a)) * 8 + a] = (uint8_t)(lo[a] != hi[a] ? kMixed : lo[a]);
+            for (int k = 0; k < 2; ++k) {
+                const int a = 2 * pair + k;
+                B.cell_field[(cbase + node_offset(P, a)) * 8 + a] = (uint8_t)(lo[k] != hi[k] ? kMixed : lo[k]);
+            }
+        }
     }
 }
 
@@ -1179,8 +1251,8 @@ void launch_register(const bm_solver* s, const int64_t* field_codes, int force, 
     k_register_particles<<<gp, kBlock, 0, st>>>(P, s->B, field_codes);
     k_register_cells<<<gc, kBlock, 0, st>>>(P, s->B);
     // incremental registration (mode 2): a few hundred nodes and cells at most per substep
-    k_register_nodes_listed<<<152, 128, 0, st>>>(P, s->B, field_codes);
-    k_register_cells_listed<<<152, 128, 0, st>>>(P, s->B, field_codes);
+    k_register_nodes_listed<<<152, kBlock, 0, st>>>(P, s->B, field_codes);
+    k_register_cells_listed<<<152, kBlock, 0, st>>>(P, s->B, field_codes);
     k_register_finish<<<gn, kBlock, 0, st>>>(P, s->B);
     k_register_reset<<<1, 1, 0, st>>>(s->B);
 }

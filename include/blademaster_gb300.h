@@ -217,6 +217,7 @@ typedef struct bm_buffers {
 #define BM_FLAG_REG_NODES 20     /* entries of buffers.reg_nodes */
 #define BM_FLAG_REG_CELLS 21     /* entries of buffers.reg_cells */
 #define BM_FLAG_HOST_DIRTY 22    /* 1 after a host write that needs a full registration */
+#define BM_FLAG_PAIR_SPEED 23    /* float bits: largest particle speed, found by a full pair-list build */
 #define BM_FLAG_WORDS 24
 
 typedef struct bm_solver bm_solver;
