@@ -357,6 +357,90 @@ def run_learned(args, rank, world):
         dist.destroy_process_group()
 
 
+# MLS-MPM step: per particle P2G reads x, v, C, F, damage + impulse (112 B); G2P reads x, F, yield,
+# damage, damage_ref (60 B) and writes x, v, C, F, damage, yield (104 B); per touched dense-grid node 56 B.
+MLS_BYTES = (276, 56)
+
+
+def run_mls(args, rank, world):
+    """The MLS-MPM baseline step at the block's scale (1.6 M particles, 2 mm grid, dt 10 us): one held
+    knife 1 mm into the top face, one 1 ms interval (100 substeps) per step, replayed as one graph."""
+    import torch
+
+    from blademaster_gb300 import replicas, scenes, _native
+    from blademaster_gb300.coupling import ToolState
+    from blademaster_gb300.mlsmpm import MlsSolver
+
+    dist, rank, world, local = replicas.init()
+    torch.cuda.set_device(local)
+    cfg, knives, _ = scenes.block_8knives()
+    s = MlsSolver(cfg, device=f"cuda:{local}")
+    knife = ToolState(knives[3], [0.0, 0.0, 0.0, 1.0], [0.0, 0.0, -0.05], [0.0, 0.0, 0.0])
+    per_step = args.substeps or 100
+    s.advance(knife, per_step * cfg.dt)  # captures and uploads the interval graph
+    graph = s.graphs[per_step]
+    for _ in range(args.warmup):
+        _native.check(s._lib.bm_graph_launch(graph, s._stream))
+    torch.cuda.synchronize()
+    clock_file = tempfile.NamedTemporaryFile(suffix=".csv", delete=False).name
+    sampler = sample_clocks(clock_file)
+    time.sleep(0.5)
+    replicas.barrier(dist, torch.cuda.current_device())
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        _native.check(s._lib.bm_graph_launch(graph, s._stream))
+    end.record()
+    replicas.barrier(dist, torch.cuda.current_device())
+    if sampler:
+        time.sleep(0.3)
+        sampler.terminate()
+        sampler.wait()
+    ms = replicas.max_over_ranks(dist, start.elapsed_time(end), torch.cuda.current_device())
+    count = ctypes.c_int64()
+    _native.check(s._lib.bm_graph_kernel_count(graph, ctypes.byref(count)))
+    substeps = args.steps * per_step
+    touched = int((s._t["grid_mass"] != 0).sum().item())
+    algo = MLS_BYTES[0] * s.n + MLS_BYTES[1] * touched
+    rate = algo / (ms / substeps * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    diag = s.diagnostics()
+    line = {
+        "metric": METRIC, "value": world * s.n * substeps / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mls_block_1p6M", "particles": s.n, "grid_nodes": int(np.prod(s.dims)),
+                   "touched_nodes": touched, "substeps_per_step": per_step, "dt_s": cfg.dt,
+                   "step": f"one {per_step * cfg.dt * 1e3:g} ms interval of the held knife, one graph replay",
+                   "l2": "inputs larger than L2 (particle state > 400 MB per substep), no flush",
+                   "parallelism": f"replicas x{world}"},
+        "ms_per_substep": ms / substeps,
+        "gpu_launches": args.steps * count.value,
+        "roofline": {"kernel": "whole MLS-MPM substep", "bound": "hbm", "achieved": rate, "peak": peak,
+                     "unit": "GB/s", "frac": rate / peak, "peak_kind": f"of {peak_kind}",
+                     "algorithmic_bytes": algo, "traffic": None},
+        "left_domain": diag["left_domain"], "clamped_inversions": diag["clamped_inversions"],
+    }
+    line["clocks"] = summarize_clocks(clock_file, torch.cuda.current_device()) if sampler else None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle.oracle import MlsOracle
+
+        o = MlsOracle(cfg)
+        o.advance(knife.position, knife.orientation_xyzw, knife.linear_velocity, knife.angular_velocity, 1)
+        steps, begin = 0, time.perf_counter()
+        while time.perf_counter() - begin < args.cpu_seconds:
+            o.advance(knife.position, knife.orientation_xyzw, knife.linear_velocity, knife.angular_velocity, 1)
+            steps += 1
+        elapsed = time.perf_counter() - begin
+        line["cpu_baseline"] = {"value": o.n * steps / elapsed, "unit": UNIT, "cores": o.L.orc_num_threads(),
+                                "kind": "port", "sample": f"{steps} MLS-MPM substeps of the full {o.n}-particle "
+                                                          "workload after 1 untimed substep, C oracle with OpenMP"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -413,6 +497,9 @@ def main():
         return
     if args.workload == "learned_c5":
         run_learned(args, rank, world)
+        return
+    if args.workload == "mls_block_1p6M":
+        run_mls(args, rank, world)
         return
     run_scene(args)
 

@@ -4,14 +4,15 @@
 // with an optional bias + ReLU epilogue and a bf16 copy of the result.
 //
 // One CTA of 128 threads computes a 128-row tile with all N (<= 256)
-// columns.  K is walked in chunks of 32: the threads stage the chunk of A
-// (128 x 32) and B (N x 32) in shared memory in the canonical no-swizzle
-// K-major layout (8 x 16-byte core matrices), make it visible to the tensor
-// core (fence.proxy.async), and one thread issues two tcgen05.mma of K = 16
-// and commits them to an mbarrier that every thread waits on before the
-// chunk's shared memory is reused.  The waits are bounded: on a timeout the
-// kernel records status 1, waits (bounded) for its MMAs, frees its tensor
-// memory and returns.  The epilogue reads the accumulator with
+// columns.  K is walked in chunks of 32 through two shared-memory stages:
+// the threads stage the chunk of A (128 x 32) and B (N x 32) in the
+// canonical no-swizzle K-major layout (8 x 16-byte core matrices), make it
+// visible to the tensor core (fence.proxy.async), and one thread issues two
+// tcgen05.mma of K = 16 and commits them to the stage's mbarrier; the next
+// chunk is staged into the other stage while those MMAs run, and a stage is
+// reused only after the commit of the chunk that last read it.  The waits are
+// bounded: on a timeout the kernel records status 1 (2 if the final wait for
+// the MMAs in flight also runs out), frees its tensor memory and returns.  The epilogue reads the accumulator with
 // tcgen05.ld (warp w owns rows 32 w .. 32 w + 31).
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -27,6 +28,7 @@ constexpr int kChunkK = 32;
 constexpr int kCoreBytes = 128;                       // 8 rows x 16 bytes
 constexpr int kChunkRowGroupBytes = (kChunkK / 8) * kCoreBytes;  // SBO: one 8-row group of a chunk
 constexpr long long kWaitLimit = 1 << 24;
+constexpr int kStageBytes = kTileM * kChunkK * 2 + 256 * kChunkK * 2;  // A tile + the widest B tile: 24 KB
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -82,10 +84,8 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
                                                  float* __restrict__ D, int M, int N, int K, const float* bias,
                                                  int relu, uint16_t* Dh, int32_t* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmem_slot;
-    uint8_t* a_tile = smem;                                   // 128 x 32 bf16 = 8 KB
-    uint8_t* b_tile = smem + kTileM * kChunkK * 2;            // N x 32 bf16 <= 16 KB
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTileM;
     const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[1])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -104,11 +105,27 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
     const uint32_t idesc = instr_desc(kTileM, N);
-    uint32_t phase = 0;
+    // Two operand stages: the threads stage chunk c into stage c & 1 while the
+    // tensor core still multiplies chunk c - 1 from the other stage; before
+    // reusing a stage they wait for the commit of the chunk that last read it.
+    uint32_t phase[2] = {0u, 0u};
+    int pending[2] = {0, 0};  // a commit on this stage's barrier not yet waited for (same in every thread)
+    const int chunks = K / kChunkK;
     bool ok = true;
-    for (int k0 = 0; k0 < K && ok; k0 += kChunkK) {
-        stage(a_tile, A, K, m0, kTileM, M, k0);
-        stage(b_tile, B, K, 0, N, N, k0);
+    for (int c = 0; c < chunks; ++c) {
+        const int st = c & 1;
+        uint8_t* a_tile = smem + st * kStageBytes;           // 128 x 32 bf16 = 8 KB
+        uint8_t* b_tile = a_tile + kTileM * kChunkK * 2;      // N x 32 bf16 <= 16 KB
+        if (pending[st]) {
+            const bool arrived = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            ok = __syncthreads_and(arrived) != 0;  // the same decision in every thread
+            if (!ok) break;
+            phase[st] ^= 1u;
+            pending[st] = 0;
+        }
+        stage(a_tile, A, K, m0, kTileM, M, c * kChunkK);
+        stage(b_tile, B, K, 0, N, N, c * kChunkK);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -118,7 +135,7 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
                 // two core matrices along K per MMA: the K-step is 2 x 128 bytes
                 const uint64_t ad = smem_desc(smem_u32(a_tile) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
                 const uint64_t bd = smem_desc(smem_u32(b_tile) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
-                const uint32_t accumulate = (k0 + kk) > 0 ? 1u : 0u;
+                const uint32_t accumulate = (c * kChunkK + kk) > 0 ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
@@ -127,18 +144,23 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
                     : "memory");
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&bar))
+                             smem_u32(&bar[st]))
                          : "memory");
         }
-        const bool arrived = mbar_wait_bounded(smem_u32(&bar), phase);
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        ok = __syncthreads_and(arrived) != 0;  // the same decision in every thread
+        pending[st] = 1;
     }
-    if (!ok) {
-        // record the timeout and give the MMAs in flight a last bounded wait before freeing their memory
-        if (threadIdx.x == 0) atomicExch(status, 1);
-        mbar_wait_bounded(smem_u32(&bar), phase ^ 1u);
+    // Drain the commits not yet waited for (also after a timeout: every MMA
+    // in flight gets a bounded wait before its tensor memory is freed).
+    bool drained = true;
+#pragma unroll
+    for (int st = 0; st < 2; ++st)
+        if (pending[st]) drained = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]) && drained;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    drained = __syncthreads_and(drained) != 0;
+    if (!ok || !drained) {
+        // status 1: a wait ran out; 2: the last wait ran out too, so the
+        // tensor memory is freed with MMAs possibly still in flight
+        if (threadIdx.x == 0) atomicMax(status, drained ? 1 : 2);
     } else {
         // epilogue: warp w reads rows 32 w + lane, 32 columns at a time
         const int row = m0 + 32 * warp + lane;
@@ -350,12 +372,10 @@ int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N
     // 96 KB per CTA keeps at most two CTAs on an SM, so their tensor-memory
     // allocations (at most 256 columns each) always fit the SM's 512 columns.
     const size_t smem = 96 * 1024;
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(bm::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return bm::check_cuda("gemm_tn_bf16 shared memory");
-        configured = true;
-    }
+    // a per-function attribute of the current device: set on every call (a cheap host call), so a
+    // first launch on any device finds it set
+    if (cudaFuncSetAttribute(bm::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return bm::check_cuda("gemm_tn_bf16 shared memory");
     bm::k_gemm_tn<<<grid, 128, smem, reinterpret_cast<cudaStream_t>(stream)>>>(A, B, D, M, N, K, bias, relu, D_bf16,
                                                                                  status);
     return bm::check_cuda("gemm_tn_bf16");
