@@ -21,6 +21,7 @@ from . import _native
 
 IN, HIDDEN, OUT = 81, 256, 6
 IN_PAD, OUT_PAD = 96, 16  # GEMM K multiple of 32 for the input, N multiple of 16 for the output
+OUT_WITH_STATE = 12  # the wrench and the knife's twist change over the interval
 LAYERS = ((HIDDEN, IN_PAD), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (OUT_PAD, HIDDEN))  # (out, in) of each weight
 
 
@@ -31,16 +32,19 @@ def _p(t):
 class ToolPredictor:
     """The MLP with its training state; tensors live on `device`."""
 
-    def __init__(self, device="cuda:0", seed=0):
+    def __init__(self, device="cuda:0", seed=0, outputs=OUT):
         import torch
 
+        if not 1 <= outputs <= OUT_PAD:
+            raise ValueError(f"outputs must be in [1, {OUT_PAD}]")
+        self.outputs = outputs
         self.device = torch.device(device)
         self._lib = _native.lib()
         rng = np.random.default_rng(seed)
         self.w, self.b, self.wh, self.wt = [], [], [], []
         for i, (fan_out, fan_in) in enumerate(LAYERS):
             real_in = IN if i == 0 else fan_in
-            real_out = OUT if i == len(LAYERS) - 1 else fan_out
+            real_out = outputs if i == len(LAYERS) - 1 else fan_out
             w = np.zeros((fan_out, fan_in), np.float32)
             w[:real_out, :real_in] = rng.normal(0.0, math.sqrt(2.0 / real_in), (real_out, real_in))
             self.w.append(torch.as_tensor(w, device=self.device))
@@ -52,8 +56,8 @@ class ToolPredictor:
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.feature_mean = np.zeros(IN, np.float32)
         self.feature_std = np.ones(IN, np.float32)
-        self.target_mean = np.zeros(OUT, np.float32)
-        self.target_std = np.ones(OUT, np.float32)
+        self.target_mean = np.zeros(outputs, np.float32)
+        self.target_std = np.ones(outputs, np.float32)
         self._refresh()
 
     @property
@@ -118,7 +122,7 @@ class ToolPredictor:
         g = torch.empty(rows, OUT_PAD, dtype=torch.float32, device=dev)
         gh = torch.zeros(rows, 32, dtype=torch.int16, device=dev)  # reduction padded to 32 for dH = dY W
         gh16 = torch.empty(rows, OUT_PAD, dtype=torch.int16, device=dev)
-        _native.check(self._lib.bm_mlp_mse_grad(_p(y), _p(target), rows, OUT, OUT_PAD, _p(g), _p(gh16), _p(loss),
+        _native.check(self._lib.bm_mlp_mse_grad(_p(y), _p(target), rows, self.outputs, OUT_PAD, _p(g), _p(gh16), _p(loss),
                                                 self._stream))
         gh[:, :OUT_PAD] = gh16
         self.grads = [None] * 4
@@ -159,7 +163,7 @@ class ToolPredictor:
         return xh
 
     def fit(self, features, wrenches, epochs=200, batch=256, lr=1.0e-3, seed=0):
-        """Train on (features [S x 81], wrenches [S x 6]); returns the loss of each epoch."""
+        """Train on (features [S x 81], targets [S x outputs]); returns the loss of each epoch."""
         import torch
 
         features = np.asarray(features, np.float32)
@@ -185,11 +189,56 @@ class ToolPredictor:
         return history
 
     def predict(self, features):
-        """Force and torque [B x 6] for feature rows [B x 81]."""
+        """Outputs [B x outputs] (force and torque first) for feature rows [B x 81]."""
         y = self.forward(self._inputs(np.atleast_2d(features)))
         if int(self.status.item()):
             raise RuntimeError("tensor-core GEMM did not complete")
-        return y[:, :OUT].cpu().numpy() * self.target_std + self.target_mean
+        return y[:, : self.outputs].cpu().numpy() * self.target_std + self.target_mean
+
+
+def features_batch(solvers, states, material_top):
+    """``features`` of many solvers, their pooling kernels queued back to back and read with one copy."""
+    import torch
+
+    solvers, states = list(solvers), [st.checked() for st in states]
+    if not solvers:
+        return np.zeros((0, IN), np.float32)
+    device = solvers[0].device
+    lib = _native.lib()
+    counts = torch.zeros(len(solvers), 64, dtype=torch.int32, device=device)
+    records = np.zeros((len(solvers), _native.TOOL_F_WORDS), np.float32)
+    for i, (solver, st) in enumerate(zip(solvers, states)):
+        records[i] = _knife_record(solver, st)
+    tools = torch.as_tensor(records, device=device)
+    for i, solver in enumerate(solvers):
+        cfg = solver.config
+        _native.check(lib.bm_mlp_pool(_p(solver._t["x"]), solver.n, _p(tools[i]), cfg.grid_spacing,
+                                      cfg.blade_half_size[1], _p(counts[i]), solver._stream))
+    counts = counts.cpu().numpy()
+    return np.stack([_assemble(solver, st, material_top, c) for solver, st, c in zip(solvers, states, counts)])
+
+
+def _knife_record(solver, st):
+    """float32 knife record of the upcoming pose: orientation (words 6-9) and edge centre (15-17)."""
+    cfg = solver.config
+    record = np.zeros(_native.TOOL_F_WORDS, np.float32)
+    q = np.asarray(st.orientation_xyzw, np.float64)
+    record[0:3], record[6:10] = st.position, q
+    x, y, z, w = q
+    down = np.array([-(2 * (x * z + w * y)), -(2 * (y * z - w * x)), -(1 - 2 * (x * x + y * y))])
+    record[15:18] = np.asarray(st.position) + cfg.blade_half_size[2] * down
+    return record
+
+
+def _assemble(solver, st, material_top, counts):
+    cfg = solver.config
+    h, half_y = cfg.grid_spacing, cfg.blade_half_size[1]
+    full = (2 * h) * (0.5 * half_y) * (2 * h) / solver.volume
+    centroid = solver.reference.mean(0)
+    edge_z = st.position[2] - cfg.blade_half_size[2]
+    head = np.concatenate([np.asarray(st.position) - centroid, st.orientation_xyzw, st.linear_velocity, st.angular_velocity,
+                           [material_top - edge_z], [math.log10(cfg.young_modulus), cfg.poisson_ratio, cfg.density / 1000.0]])
+    return np.concatenate([head, counts / full]).astype(np.float32)
 
 
 def features(solver, state, material_top):
@@ -199,28 +248,7 @@ def features(solver, state, material_top):
     the cut depth (material top minus edge height), the material (log10 E,
     nu, rho / 1000) and the 64 bin occupancies (count / particles a full bin holds).
     """
-    import torch
-
-    cfg = solver.config
-    st = state.checked()
-    counts = torch.zeros(64, dtype=torch.int32, device=solver.device)
-    lib = _native.lib()
-    h, half_y = cfg.grid_spacing, cfg.blade_half_size[1]
-    # float32 knife record of the upcoming pose: orientation (words 6-9) and edge centre (15-17)
-    record = np.zeros(_native.TOOL_F_WORDS, np.float32)
-    q = np.asarray(st.orientation_xyzw, np.float64)
-    record[0:3], record[6:10] = st.position, q
-    x, y, z, w = q
-    down = np.array([-(2 * (x * z + w * y)), -(2 * (y * z - w * x)), -(1 - 2 * (x * x + y * y))])
-    record[15:18] = np.asarray(st.position) + cfg.blade_half_size[2] * down
-    tool = torch.as_tensor(record, device=solver.device)
-    _native.check(lib.bm_mlp_pool(_p(solver._t["x"]), solver.n, _p(tool), h, half_y, _p(counts), solver._stream))
-    full = (2 * h) * (0.5 * half_y) * (2 * h) / solver.volume
-    centroid = solver.reference.mean(0)
-    edge_z = st.position[2] - cfg.blade_half_size[2]
-    head = np.concatenate([np.asarray(st.position) - centroid, st.orientation_xyzw, st.linear_velocity, st.angular_velocity,
-                           [material_top - edge_z], [math.log10(cfg.young_modulus), cfg.poisson_ratio, cfg.density / 1000.0]])
-    return np.concatenate([head, counts.cpu().numpy() / full]).astype(np.float32)
+    return features_batch([solver], [state], material_top)[0]
 
 
 class GatedPredictor:

@@ -89,3 +89,30 @@ def test_gpu_constraint_matches_oracle(angle):
     # entry sides, both in device (cell-sorted) order
     np.testing.assert_array_equal(g._t["hold"][0].cpu().numpy(), o.arrays["hold_side"])
     assert g.blade_constraint.max_violation <= 1.0e-6
+
+
+@pytest.mark.gpu
+def test_sweep_instance_that_does_not_converge_fails_like_the_oracle():
+    # Instance 69 of the seeded cylinder sweep (4 mm grid, E = 3.2e5 Pa, 0.13 m/s): at
+    # interval 12 the solve ends its 8 batches of 48 iterations at 2.35e-6 m/s.  The oracle
+    # ends at the same residual, and the port raises as the reference's does
+    # (coupling.py:187-188); the residual is a lifetime maximum, so later intervals raise too.
+    from blademaster_gb300 import scenes
+    from blademaster_gb300.solver import Solver
+    from blademaster_gb300.sweep import instances
+
+    inst = instances(256, seed=0)[69]
+    s, o = Solver(inst.config), OracleSolver(inst.config)
+    port = ExternalToolPort(s)
+    steps = int(round(0.001 / inst.config.dt))
+    for k in range(13):
+        state = inst.state(k, start_gap=-0.001)
+        impulse, _, _ = o.external_interval(scenes.packed_state(state), steps, True, 0)
+        if k < 12:
+            reaction = port.advance(state, 0.001)
+            np.testing.assert_array_equal(reaction.impulse_ns, impulse, err_msg=f"interval {k}")
+        else:
+            with pytest.raises(RuntimeError, match="did not converge"):
+                port.advance(state, 0.001)
+    residual = np.int32(o.arrays["flags"][_native.FLAG["HOLD_RESIDUAL"]]).view(np.float32)
+    assert s.blade_constraint.max_violation == float(residual) > 1.0e-6
