@@ -419,6 +419,52 @@ def run_learned(args, rank, world):
         dist.destroy_process_group()
 
 
+def run_triple_cut(args, rank, world):
+    """The triple cut of the Maxwell cylinder through ExternalToolPort, as the reference's scenarios
+    drive it: one step = one 2 ms coupling interval (32 substeps, one graph replay and one readback
+    of the interval's impulses).  The warm-up intervals run from t = 0; the solver is then restored
+    to t = 0 and the first `--steps` intervals of the schedule are timed on the host clock around
+    each port call (whole-job, device-synchronised by the readback)."""
+    import torch
+
+    from blademaster_gb300 import replicas, scenes
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.solver import Solver
+
+    dist, rank, world, local = replicas.init()
+    torch.cuda.set_device(local)
+    cfg = scenes.triple_cut_config()
+    s = Solver(cfg, device=f"cuda:{local}")
+    port = ExternalToolPort(s)
+    schedule = scenes.triple_cut_schedule()
+    steps = min(args.steps, len(schedule))
+    start_of_run = s.checkpoint()
+    for state, cutting, index in schedule[: max(args.warmup, 3)]:
+        port.advance(state, scenes.TRIPLE_CUT_INTERVAL, cutting=cutting, cut_index=index)
+    s.restore(start_of_run)
+    torch.cuda.synchronize()
+    replicas.barrier(dist, torch.cuda.current_device())
+    begin = time.perf_counter()
+    for state, cutting, index in schedule[:steps]:
+        port.advance(state, scenes.TRIPLE_CUT_INTERVAL, cutting=cutting, cut_index=index)
+    seconds = replicas.max_over_ranks(dist, time.perf_counter() - begin, torch.cuda.current_device())
+    per = int(round(scenes.TRIPLE_CUT_INTERVAL / cfg.dt))
+    simulated = steps * scenes.TRIPLE_CUT_INTERVAL
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": world * s.n * per * steps / seconds, "unit": UNIT, "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": seconds / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "triple_cut_4480", "particles": s.n, "substeps_per_step": per, "dt_s": cfg.dt,
+                       "schedule_intervals": len(schedule),
+                       "step": "one 2 ms ExternalToolPort.advance (graph replay + interval readback) from t = 0"},
+            "wall_s_per_simulated_s": seconds / simulated,
+            "parallelism": f"replicas x{world}",
+        }), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 # MLS-MPM step: per particle P2G reads x, v, C, F, damage + impulse (112 B); G2P reads x, F, yield,
 # damage, damage_ref (60 B) and writes x, v, C, F, damage, yield (104 B); per touched dense-grid node 56 B.
 MLS_BYTES = (276, 56)
@@ -543,6 +589,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="launch substeps without CUDA graphs (profiling)")
+    ap.add_argument("--profile-window", type=int, default=-1,
+                    help="profiling: advance this many substeps from t = 0 (graphs), then run --profile-steps eager "
+                         "substeps inside a CUDA profiler range (for ncu --profile-from-start off) and exit")
     ap.add_argument("--instances", type=int, default=256, help="instances of the sweep_c4 workload")
     ap.add_argument("--learned-instances", type=int, default=256, help="training instances of the learned_c5 workload")
     ap.add_argument("--learned-intervals", type=int, default=800, help="training intervals per learned_c5 instance")
@@ -565,7 +614,42 @@ def main():
     if args.workload == "mls_block_1p6M":
         run_mls(args, rank, world)
         return
+    if args.workload == "triple_cut_4480":
+        run_triple_cut(args, rank, world)
+        return
+    if args.profile_window >= 0:
+        run_profile_window(args)
+        return
     run_scene(args)
+
+
+def run_profile_window(args):
+    """Eager substeps of a scene workload at a given time, inside a CUDA profiler range."""
+    import torch
+
+    from blademaster_gb300 import _native
+    from blademaster_gb300.solver import Solver
+
+    cfg, knives, velocity = workload(args.workload)
+    s = Solver(cfg)
+    s.tool_pos.assign(knives)
+    s.tool_vel.assign(velocity)
+    per = SUBSTEPS_PER_STEP.get(args.workload, 100)
+    done = 0
+    while done < args.profile_window:
+        k = min(per, args.profile_window - done)
+        s.advance(np.zeros((k, 3)), cutting=True)
+        done += k
+    torch.cuda.synchronize()
+    before = s._t["flags"].cpu().numpy().copy()
+    torch.cuda.profiler.start()
+    s.advance(np.zeros((args.profile_steps, 3)), cutting=True, graph=False)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    after = s._t["flags"].cpu().numpy()
+    events = {k: int(after[_native.FLAG[k]] - before[_native.FLAG[k]]) for k in ("PAIR_BUILDS", "RELISTS", "REGISTRATIONS")}
+    print(json.dumps({"workload": args.workload, "particles": s.n, "window_start": args.profile_window,
+                      "eager_substeps": args.profile_steps, "events": events}), flush=True)
 
 
 def run_scene(args):
