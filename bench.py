@@ -385,6 +385,24 @@ def run_learned(args, rank, world):
     sync()
     forward_s = (time.perf_counter() - t0) / 20
     flops = 2 * 32768 * (96 * 256 + 2 * 256 * 256 + 256 * 16)
+    # the tcgen05 GEMM alone (hidden-layer shape, bf16 operands, fp32 out), CUDA events on its stream
+    import torch
+    gemm_rates = {}
+    for rows_g in (32768, 131072):
+        a = torch.randn(rows_g, 256, device=f"cuda:{local}").to(torch.bfloat16).view(torch.int16)
+        b = torch.randn(256, 256, device=f"cuda:{local}").to(torch.bfloat16).view(torch.int16)
+        d = torch.empty(rows_g, 256, dtype=torch.float32, device=f"cuda:{local}")
+        for _ in range(5):
+            gemm._gemm(a, b, rows_g, 256, 256, D=d)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(50):
+            gemm._gemm(a, b, rows_g, 256, 256, D=d)
+        e1.record()
+        sync()
+        gemm_ms = e0.elapsed_time(e1) / 50
+        gemm_rates[f"{rows_g}x256x256"] = {"us": gemm_ms * 1e3, "tflops": 2 * rows_g * 256 * 256 / (gemm_ms * 1e-3) / 1e12}
+    gemm_status = int(gemm.status.item())
     learned_s = replicas.max_over_ranks(dist, learned_s)
     plain_s = replicas.max_over_ranks(dist, plain_s)
     held_work = replicas.sum_over_ranks(dist, work * intervals)
@@ -413,6 +431,7 @@ def run_learned(args, rank, world):
                         "held_out_failed_instance_intervals": failures},
             "mlp_forward": {"rows": 32768, "ms": forward_s * 1e3, "tflops": flops / forward_s / 1e12,
                             "frac_of_bf16_burst": flops / forward_s / 1e12 / peak_tf},
+            "gemm_tn_bf16": {**gemm_rates, "status": gemm_status, "peak_bf16_tflops": peak_tf},
             "parallelism": f"replicas x{world}, {count} instances per rank",
         }), flush=True)
     if dist:

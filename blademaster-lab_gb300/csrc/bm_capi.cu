@@ -113,7 +113,7 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         bm::launch_rigid(s, a->cut_bits, st);
         t.mark(2, st);
         // The knife integration needs only this substep's reactions and is read
-        // only by the F update / side labels and the next substep, so (outside
+        // only by the side labels and the next substep, so (outside
         // external mode, where the grid constraint may still change the
         // reaction) it runs on a side stream concurrently with the transfers.
         int mode = bm::kToolDrive;
@@ -137,15 +137,26 @@ int run_batch(bm_solver* s, const bm_step_args* a, cudaStream_t st, StageTimer* 
         if (P.external_tool && !P.predict) bm::launch_hold(s, st);
         t.mark(5, st);
         bm::launch_g2p(s, st);
+        // The side labels read the knife after its step and x, v after G2P; they
+        // write only codes and the next substep's relist and registration work
+        // lists, which neither the remap nor the F update reads.  Outside
+        // profiling they run on the side stream after the knife, beside those
+        // passes, and the next substep starts after both.
+        if (fork) {
+            cudaEventRecord(s->labels_fork, st);
+            cudaStreamWaitEvent(s->side, s->labels_fork, 0);
+            bm::launch_assign(s, a->cut_index, a->cut_bits != 0, s->side);
+            cudaEventRecord(s->join, s->side);
+        }
         t.mark(6, st);
         bm::launch_remap(s, st, overlap ? s->aux : nullptr);
         t.mark(7, st);
-        if (fork) cudaStreamWaitEvent(st, s->join, 0);
-        else bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
+        if (!fork) bm::launch_tool_step(s, mode, a->use_targets ? i : 0, 1, st);
         t.mark(8, st);
         bm::launch_fupdate(s, 1, 1, st);
         t.mark(9, st);
-        bm::launch_assign(s, a->cut_index, a->cut_bits != 0, st);
+        if (fork) cudaStreamWaitEvent(st, s->join, 0);
+        else bm::launch_assign(s, a->cut_index, a->cut_bits != 0, st);
         t.mark(10, st);
         if (t.on) {
             if (cudaEventSynchronize(t.ev[BM_STAGES]) != cudaSuccess) return check_cuda("profiled substep");
@@ -228,13 +239,14 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
     layout_scratch(s);
     s->side = s->aux = s->lists = nullptr;
     s->fork = s->join = s->register_fork = s->register_join = s->aux_fork = s->aux_join = nullptr;
-    s->lists_fork = s->lists_join = nullptr;
+    s->lists_fork = s->lists_join = s->labels_fork = nullptr;
     if (cudaMemset(s->B.scratch + 1, 0, 63 * sizeof(int32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->lists, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->lists_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->lists_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->labels_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->aux_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->aux_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -245,7 +257,7 @@ int bm_solver_create(const bm_params* params, const bm_buffers* buffers, bm_solv
         for (cudaStream_t q : {s->side, s->aux, s->lists})
             if (q) cudaStreamDestroy(q);
         for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join,
-                              s->lists_fork, s->lists_join})
+                              s->lists_fork, s->lists_join, s->labels_fork})
             if (e) cudaEventDestroy(e);
         delete s;
         return rc;
@@ -261,7 +273,7 @@ int bm_solver_destroy(bm_solver* s) {
         cudaStreamDestroy(q);
     }
     for (cudaEvent_t e : {s->fork, s->join, s->register_fork, s->register_join, s->aux_fork, s->aux_join,
-                          s->lists_fork, s->lists_join})
+                          s->lists_fork, s->lists_join, s->labels_fork})
         cudaEventDestroy(e);
     delete s;
     return BM_OK;

@@ -15,7 +15,7 @@ struct bm_solver {
     cudaStream_t side;       // registration and knife integration run here, beside the main chain
     cudaStream_t aux;        // the multi-field node passes run here, beside the single-field ones
     cudaStream_t lists;      // the pair-list build and relists run here, beside the contact pass
-    cudaEvent_t fork, join, register_fork, register_join, aux_fork, aux_join, lists_fork, lists_join;
+    cudaEvent_t fork, join, register_fork, register_join, aux_fork, aux_join, lists_fork, lists_join, labels_fork;
 };
 
 struct bm_graph {
