@@ -610,7 +610,8 @@ def main():
     ap.add_argument("--eager", action="store_true", help="launch substeps without CUDA graphs (profiling)")
     ap.add_argument("--profile-window", type=int, default=-1,
                     help="profiling: advance this many substeps from t = 0 (graphs), then run --profile-steps eager "
-                         "substeps inside a CUDA profiler range (for ncu --profile-from-start off) and exit")
+                         "substeps inside a CUDA profiler range (for ncu --profile-from-start off) and exit; "
+                         "for triple_cut_4480 this many 2 ms port intervals, then one eager interval")
     ap.add_argument("--instances", type=int, default=256, help="instances of the sweep_c4 workload")
     ap.add_argument("--learned-instances", type=int, default=256, help="training instances of the learned_c5 workload")
     ap.add_argument("--learned-intervals", type=int, default=800, help="training intervals per learned_c5 instance")
@@ -633,11 +634,11 @@ def main():
     if args.workload == "mls_block_1p6M":
         run_mls(args, rank, world)
         return
-    if args.workload == "triple_cut_4480":
-        run_triple_cut(args, rank, world)
-        return
     if args.profile_window >= 0:
         run_profile_window(args)
+        return
+    if args.workload == "triple_cut_4480":
+        run_triple_cut(args, rank, world)
         return
     run_scene(args)
 
@@ -649,6 +650,26 @@ def run_profile_window(args):
     from blademaster_gb300 import _native
     from blademaster_gb300.solver import Solver
 
+    if args.workload == "triple_cut_4480":
+        # the window counts 2 ms port intervals; the profiled one runs its 32 substeps eagerly
+        from blademaster_gb300 import scenes
+        from blademaster_gb300.coupling import ExternalToolPort
+
+        s = Solver(scenes.triple_cut_config())
+        port = ExternalToolPort(s)
+        schedule = scenes.triple_cut_schedule()
+        for state, cutting, index in schedule[:args.profile_window]:
+            port.advance(state, scenes.TRIPLE_CUT_INTERVAL, cutting=cutting, cut_index=index)
+        state, cutting, index = schedule[args.profile_window]
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        port.advance(state, scenes.TRIPLE_CUT_INTERVAL, cutting=cutting, cut_index=index, graph=False)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"workload": args.workload, "particles": s.n, "window_start_interval": args.profile_window,
+                          "cutting": bool(cutting), "cut_index": int(index),
+                          "eager_substeps": int(round(scenes.TRIPLE_CUT_INTERVAL / s.config.dt))}), flush=True)
+        return
     cfg, knives, velocity = workload(args.workload)
     s = Solver(cfg)
     s.tool_pos.assign(knives)

@@ -501,6 +501,12 @@ __global__ void k_pair_begin(bm_params P, bm_buffers B, int64_t buckets, const i
     const int N = P.n;
     float d = 0.0f;
     const float inf = __int_as_float(0x7f800000);
+    // the speed maximum as the contact pass forms it (a NaN speed wins there
+    // too): warp maxima, combined by integer maximum of their bit patterns,
+    // here over the warp's grid-stride iterations first and then by one
+    // atomic per warp (the same value as one atomic per iteration)
+    int speed_bits = 0;
+    bool speed_any = false;
     for (int p0 = blockIdx.x * blockDim.x; p0 < N; p0 += gridDim.x * blockDim.x) {
         const int p = p0 + threadIdx.x;
         const bool active = p < N;
@@ -509,15 +515,15 @@ __global__ void k_pair_begin(bm_params P, bm_buffers B, int64_t buckets, const i
             d = fmaxf(d, v3_len(v3_sub(ld3(B.x, N, p), ld3(B.ref, N, p))));
             if (find_speed) speed = v3_len(ld3(B.v, N, p));
         }
-        if (find_speed) {  // block-uniform
-            // the same maximum as the contact pass's (a NaN speed wins there too);
-            // every lane takes part in both warp collectives
+        if (find_speed) {  // block-uniform; every lane takes part in both warp collectives
             const float vmax = warp_max(speed);
-            const bool any = __any_sync(0xffffffffu, active);
-            if ((threadIdx.x & 31) == 0 && any)
-                atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_PAIR_SPEED]), vmax);
+            if (__any_sync(0xffffffffu, active)) {
+                speed_bits = max(speed_bits, __float_as_int(vmax));
+                speed_any = true;
+            }
         }
     }
+    if ((threadIdx.x & 31) == 0 && speed_any) atomicMax(&B.flags[BM_FLAG_PAIR_SPEED], speed_bits);
     for (int s = 16; s > 0; s >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, s));
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(reinterpret_cast<float*>(&B.flags[BM_FLAG_MAX_DISP]), d);
 }
@@ -957,7 +963,8 @@ void launch_prologue(const bm_solver* s, int clear_step, cudaStream_t st, int re
 }
 
 void launch_rigid(const bm_solver* s, int cut_bits, cudaStream_t st) {
-    k_rigid<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, cut_bits);
+    const int tb = spread_block(s->P.n);
+    k_rigid<<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, cut_bits);
 }
 
 void launch_pairs(const bm_solver* s, cudaStream_t st) { launch_pairs_using(s, s->scan_partials, st); }

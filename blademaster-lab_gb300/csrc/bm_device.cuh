@@ -13,6 +13,7 @@
 namespace bm {
 
 constexpr int kBlock = 256;
+constexpr int kSMs = 152;  // streaming multiprocessors of a GB300
 
 // Structure-of-arrays access with 32-bit indices (every array here holds
 // fewer than 2^31 elements: n < 2^28 particles, fmax * node_count < 2^29).
@@ -266,6 +267,19 @@ __device__ __forceinline__ void begin_registration(const bm_buffers& B, int forc
 inline unsigned grid_for(int64_t count, int block = kBlock) {
     int64_t g = (count + block - 1) / block;
     return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Threads per block of a one-thread-per-item launch: kBlock, or fewer (a
+// power of two, at least one warp) when kBlock-sized blocks would not give
+// every SM a block.  A small scene's warps then spread over the SMs instead
+// of queueing several to an SM, which matters for the float64 Maxwell
+// update (its warps share an SM's few FP64 lanes) and the long per-particle
+// chains of the contact pass.  Kernels launched this way use no block-wide
+// shared memory or barrier, only warp-level collectives.
+inline int spread_block(int64_t count) {
+    int threads = 32;
+    while (threads < kBlock && (count + threads - 1) / threads > kSMs) threads *= 2;
+    return threads;
 }
 
 }  // namespace bm

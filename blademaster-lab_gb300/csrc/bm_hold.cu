@@ -303,7 +303,8 @@ void launch_hold(const bm_solver* s, cudaStream_t st) {
     const int32_t* gate = &B.flags[BM_FLAG_HOLD_NEEDS];
     const unsigned wide = 4 * 152;
     const unsigned gn = grid_for(P.n) < wide ? grid_for(P.n) : wide;
-    k_hold_prepare<<<grid_for(P.n), kBlock, 0, st>>>(P, B);
+    const int tb = spread_block(P.n);
+    k_hold_prepare<<<grid_for(P.n, tb), tb, 0, st>>>(P, B);
     launch_exclusive_scan(B.hold_mark, B.hold_pos, P.n, s->scan_partials, &B.flags[BM_FLAG_HOLD_COUNT], scan_ticket(B), gate,
                           st);
     k_hold_list<<<gn, kBlock, 0, st>>>(P, B);

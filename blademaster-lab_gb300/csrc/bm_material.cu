@@ -1279,7 +1279,8 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st, cudaSt
     const bm_buffers& B = s->B;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     const int sums = P.viscous ? 1 : write_sums;
-    k_p2g_cells<<<grid_for(cells8), kBlock, 0, st>>>(P, B);
+    const int tc = spread_block(cells8);
+    k_p2g_cells<<<grid_for(cells8, tc), tc, 0, st>>>(P, B);
     fork_aux(s, st, aux, [&](cudaStream_t q) { k_p2g_multi<<<4 * 152, kBlock, 0, q>>>(P, B, sums); });
     k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, sums);
     join_aux(s, st, aux);
@@ -1298,7 +1299,8 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st, cudaSt
 void launch_g2p(const bm_solver* s, cudaStream_t st) {
     const bm_params& P = s->P;
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
-    k_g2p<<<grid_for(cells8), kBlock, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
+    const int tc = spread_block(cells8);
+    k_g2p<<<grid_for(cells8, tc), tc, 0, st>>>(P, s->B, 0.5f * P.pair_skin, P.pair_search == 0 ? 1 : 0);
 }
 
 void launch_remap(const bm_solver* s, cudaStream_t st, cudaStream_t aux) {
@@ -1309,11 +1311,13 @@ void launch_remap(const bm_solver* s, cudaStream_t st, cudaStream_t aux) {
 }
 
 void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st) {
-    if (do_update || advance_step) k_fupdate<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, do_update, advance_step);
+    const int tb = spread_block(s->P.n);
+    if (do_update || advance_step) k_fupdate<<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, do_update, advance_step);
 }
 
 void launch_assign(const bm_solver* s, int cut_index, int cutting, cudaStream_t st) {
-    if (cutting) k_assign<<<grid_for(s->P.n), kBlock, 0, st>>>(s->P, s->B, cut_index, cutting);
+    const int tb = spread_block(s->P.n);
+    if (cutting) k_assign<<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, cut_index, cutting);
 }
 
 void launch_refresh_stress(const bm_solver* s, cudaStream_t st) {
