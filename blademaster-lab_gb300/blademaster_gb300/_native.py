@@ -178,6 +178,7 @@ def _declare(lib):
         "bm_particle_contacts_static": ([vp, vp], i),
         "bm_hold_constraint": ([vp, vp], i),
         "bm_gemm_tn_bf16": ([vp, vp, vp, i, i, i, vp, i, vp, vp, vp], i),
+        "bm_gemm_set_loop_wait_limit": ([ctypes.c_longlong], i),
         "bm_mlp_transpose16": ([vp, vp, i, i, vp], i),
         "bm_mlp_relu_grad": ([vp, vp, vp, ctypes.c_int64, vp], i),
         "bm_mlp_pool": ([vp, i, vp, f, f, vp, vp], i),

@@ -430,7 +430,10 @@ struct NodeStage {
 // 3 - g.  Every load is issued without a branch (particle 0 stands in where
 // a slot is not needed), so the cell words, the particles and the stencil
 // rows of all 64 (corner, slot) pairs take three dependent round trips.
-template <int V>
+// With kOwnCorners a uniform corner is staged from its particles too (the
+// pass then needs nothing from the cell pass and may run beside it);
+// otherwise it takes the cell pass's partial in slot 0.
+template <int V, bool kOwnCorners = false>
 __device__ __forceinline__ void stage_node(const bm_params& P, const bm_buffers& B, int n, NodeStage& st) {
     const int lane = threadIdx.x & 31, g = lane >> 3, s = lane & 7;
     const int N = P.n, NC = P.node_count, plane = 8 * NC;
@@ -445,8 +448,9 @@ __device__ __forceinline__ void stage_node(const bm_params& P, const bm_buffers&
             count = B.cell_start[c + 1] - b;
         }
         const bool mixed = flag == kMixed && s < count;
-        const bool uniform = flag != kMixed && flag != kAbsentCorner && s == 0;
-        const int p = mixed ? b + s : 0;
+        const bool uniform = flag != kMixed && flag != kAbsentCorner && (kOwnCorners ? s < count : s == 0);
+        const bool own = mixed || (kOwnCorners && uniform);  // slot s's particle is staged
+        const int p = own ? b + s : 0;
         const uint64_t fidx = B.fidx[p];
         const int sid = B.stencil_id[p];
         float e[V];
@@ -465,11 +469,12 @@ __device__ __forceinline__ void stage_node(const bm_params& P, const bm_buffers&
         const float* part = B.cell_part + a * NC + n;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-            const float u = part[v * plane];
-            st.val[a][8 * s + v] = mixed ? e[v] : (uniform ? u : 0.0f);
+            const float u = kOwnCorners ? 0.0f : part[v * plane];
+            st.val[a][8 * s + v] = own ? e[v] : (uniform ? u : 0.0f);
         }
         st.field[a][s] = mixed ? field_of(fidx, a) : (uniform ? flag : -1);
-        if (s == 0) st.flag[a] = flag;
+        // a uniform corner staged from its particles is summed like a mixed one
+        if (s == 0) st.flag[a] = (kOwnCorners && flag != kAbsentCorner) ? kMixed : flag;
     }
 }
 
@@ -855,10 +860,10 @@ __device__ __forceinline__ bm_m33 corotated_polar(const bm_m33& f, float J, floa
     return out;
 }
 
-// material.stress_at (material.py:94-112).
-__device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
+// material.stress_at (material.py:94-112) of the deformation gradient F of
+// particle p (the caller's copy of buffers.F[p]).
+__device__ __forceinline__ void stress_of(const bm_params& P, const bm_buffers& B, int p, const bm_m33& F) {
     const int N = P.n;
-    const bm_m33 F = ld9(B.F, N, p);
     bm_m33 f = F, pinv = m33_identity();
     if (P.use_fp) {
         pinv = m33_inverse(ld9(B.Fp, N, p));
@@ -873,6 +878,7 @@ __device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) {
     if (P.use_fp) st9(B.stress, N, p, m33_mul(corotated_polar(f, J, P.mu, P.lam), m33_transpose(pinv)));
     else st9(B.stress, N, p, corotated_polar(f, J, P.mu, P.lam));
 }
+__device__ void stress_at(const bm_params& P, const bm_buffers& B, int p) { stress_of(P, B, p, ld9(B.F, P.n, p)); }
 
 // material.plastic_at (material.py:404-431).
 __device__ bool plastic_at(const bm_params& P, const bm_buffers& B, int p, float yield_stress, bm_m33* U, bm_v3* s,
@@ -1116,8 +1122,13 @@ __global__ void __launch_bounds__(256) k_assign(bm_params P, bm_buffers B, int c
 }
 
 // update_F_plastic / update_F_maxwell (material.py:445-475, 592-618); thread
-// 0 advances the substep counter of the friction-history ping-pong.
-__global__ void __launch_bounds__(256, 4) k_fupdate(bm_params P, bm_buffers B, int do_update, int advance_step) {
+// 0 advances the substep counter of the friction-history ping-pong.  The
+// elastic update (kMinBlocks 4: polar stress only, launched when neither
+// plasticity nor the Maxwell element is on) runs at 4 blocks per SM (64
+// registers); the SVD-based plastic and Maxwell updates get the registers
+// their Jacobi sweeps need (kMinBlocks 1), where a 64-register cap spills them.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_fupdate(bm_params P, bm_buffers B, int do_update, int advance_step) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (advance_step && p == 0) B.flags[BM_FLAG_STEP] += 1;
     const bool active = p < P.n;
@@ -1136,8 +1147,11 @@ __global__ void __launch_bounds__(256, 4) k_fupdate(bm_params P, bm_buffers B, i
             const int s = slot_of(P, base, fidx, a);
             rate = m33_add(rate, m33_outer(ld3(B.remap_v, S, s), stencil_g(B, sid, a)));
         }
-        st9(B.F, N, p, m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt)));
-        constitutive(P, B, p);
+        const bm_m33 F = m33_add(ld9(B.F, N, p), m33_scale(rate, P.dt));
+        st9(B.F, N, p, F);
+        // the elastic stress from the new F in registers, the SVD-based laws from buffers.F
+        if (kMinBlocks == 4) stress_of(P, B, p, F);
+        else constitutive(P, B, p);
     }
 }
 
@@ -1280,6 +1294,8 @@ void launch_material(const bm_solver* s, int write_sums, cudaStream_t st, cudaSt
     const int cells8 = 8 * P.cell_dims[0] * P.cell_dims[1] * P.cell_dims[2];
     const int sums = P.viscous ? 1 : write_sums;
     const int tc = spread_block(cells8);
+    // the multi-field nodes stage every corner from the particles, so they
+    // run beside the cell pass and the single-field node pass
     k_p2g_cells<<<grid_for(cells8, tc), tc, 0, st>>>(P, B);
     fork_aux(s, st, aux, [&](cudaStream_t q) { k_p2g_multi<<<4 * 152, kBlock, 0, q>>>(P, B, sums); });
     k_p2g_grid<<<grid_for(P.active_nodes), kBlock, 0, st>>>(P, B, sums);
@@ -1312,7 +1328,11 @@ void launch_remap(const bm_solver* s, cudaStream_t st, cudaStream_t aux) {
 
 void launch_fupdate(const bm_solver* s, int do_update, int advance_step, cudaStream_t st) {
     const int tb = spread_block(s->P.n);
-    if (do_update || advance_step) k_fupdate<<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, do_update, advance_step);
+    if (!(do_update || advance_step)) return;
+    if (s->P.maxwell || s->P.plastic)
+        k_fupdate<1><<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, do_update, advance_step);
+    else
+        k_fupdate<4><<<grid_for(s->P.n, tb), tb, 0, st>>>(s->P, s->B, do_update, advance_step);
 }
 
 void launch_assign(const bm_solver* s, int cut_index, int cutting, cudaStream_t st) {

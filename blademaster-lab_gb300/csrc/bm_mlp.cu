@@ -4,16 +4,19 @@
 // with an optional bias + ReLU epilogue and a bf16 copy of the result.
 //
 // One CTA of 128 threads computes a 128-row tile with all N (<= 256)
-// columns.  K is walked in chunks of 32 through two shared-memory stages:
-// the threads stage the chunk of A (128 x 32) and B (N x 32) in the
-// canonical no-swizzle K-major layout (8 x 16-byte core matrices), make it
-// visible to the tensor core (fence.proxy.async), and one thread issues two
-// tcgen05.mma of K = 16 and commits them to the stage's mbarrier; the next
-// chunk is staged into the other stage while those MMAs run, and a stage is
-// reused only after the commit of the chunk that last read it.  The waits are
-// bounded: on a timeout the kernel records status 1 (2 if the final wait for
-// the MMAs in flight also runs out), frees its tensor memory and returns.  The epilogue reads the accumulator with
-// tcgen05.ld (warp w owns rows 32 w .. 32 w + 31).
+// columns.  K is walked in chunks of 32 through a ring of four shared-memory
+// stages: the threads copy the chunk of A (128 x 32) and B (N x 32) with
+// cp.async (16 bytes each, no register round trip) into the canonical
+// no-swizzle K-major layout (8 x 16-byte core matrices) two chunks ahead of
+// the tensor core, make a landed chunk visible to it (fence.proxy.async),
+// and one thread issues two tcgen05.mma of K = 16 and commits them to the
+// stage's mbarrier.  A stage is refilled only after the commit of the chunk
+// that last read it (two chunks earlier).  The waits are bounded: on a
+// timeout the kernel records status 1 (2 if the final wait for the MMAs in
+// flight also runs out), frees its tensor memory and returns.  The epilogue
+// reads the accumulator with tcgen05.ld (warp w owns rows 32 w .. 32 w + 31)
+// and transposes each 32 x 32 block through shared memory, so that every
+// store of D writes 32 consecutive columns of one row.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -29,6 +32,8 @@ constexpr int kCoreBytes = 128;                       // 8 rows x 16 bytes
 constexpr int kChunkRowGroupBytes = (kChunkK / 8) * kCoreBytes;  // SBO: one 8-row group of a chunk
 constexpr long long kWaitLimit = 1 << 24;
 constexpr int kStageBytes = kTileM * kChunkK * 2 + 256 * kChunkK * 2;  // A tile + the widest B tile: 24 KB
+constexpr int kStages = 4;  // 96 KB of dynamic shared memory
+constexpr int kAhead = 2;   // chunks copied ahead of the one the tensor core takes next
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -60,23 +65,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
     return done != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase) {
-    for (long long i = 0; i < kWaitLimit; ++i)
+// Poll limit of the waits inside the K loop (kWaitLimit unless a test lowers
+// it to drive the timeout path); the final drain always polls kWaitLimit.
+__device__ long long g_loop_wait_limit = kWaitLimit;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, long long limit = kWaitLimit) {
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
 
 // Stage rows [row0, row0 + rows) x columns [k0, k0 + 32) of a K-major bf16
-// matrix (row stride ld elements) into the core-matrix layout at dst;
-// rows beyond `valid` are zero.
-__device__ __forceinline__ void stage(uint8_t* dst, const uint16_t* __restrict__ src, int ld, int row0, int rows,
-                                      int valid, int k0) {
-    // one 16-byte piece (8 elements) per step: rows x 4 pieces
+// matrix (row stride ld elements) into the core-matrix layout at dst with
+// cp.async, 16 bytes per instruction straight into shared memory; rows
+// beyond `valid` are zero-filled (source size 0, from the matrix's first
+// row, which is always a valid address).
+__device__ __forceinline__ void stage_async(uint8_t* dst, const uint16_t* __restrict__ src, int ld, int row0, int rows,
+                                            int valid, int k0) {
     for (int t = threadIdx.x; t < rows * (kChunkK / 8); t += blockDim.x) {
         const int r = t >> 2, piece = t & 3;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (row0 + r < valid) v = *reinterpret_cast<const uint4*>(src + (int64_t)(row0 + r) * ld + k0 + 8 * piece);
-        *reinterpret_cast<uint4*>(dst + (r >> 3) * kChunkRowGroupBytes + piece * kCoreBytes + (r & 7) * 16) = v;
+        const bool in = row0 + r < valid;
+        const uint16_t* from = in ? src + (int64_t)(row0 + r) * ld + k0 + 8 * piece : src;
+        const uint32_t to = smem_u32(dst + (r >> 3) * kChunkRowGroupBytes + piece * kCoreBytes + (r & 7) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(to), "l"(from), "r"(in ? 16 : 0) : "memory");
     }
 }
 
@@ -84,7 +95,7 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
                                                  float* __restrict__ D, int M, int N, int K, const float* bias,
                                                  int relu, uint16_t* Dh, int32_t* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[kStages];
     __shared__ uint32_t tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTileM;
@@ -96,8 +107,8 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[1])) : "memory");
+        for (int st = 0; st < kStages; ++st)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[st])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -105,36 +116,52 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
     const uint32_t idesc = instr_desc(kTileM, N);
-    // Two operand stages: the threads stage chunk c into stage c & 1 while the
-    // tensor core still multiplies chunk c - 1 from the other stage; before
-    // reusing a stage they wait for the commit of the chunk that last read it.
-    uint32_t phase[2] = {0u, 0u};
-    int pending[2] = {0, 0};  // a commit on this stage's barrier not yet waited for (same in every thread)
     const int chunks = K / kChunkK;
+    uint32_t phase[kStages];
+    int pending[kStages];  // a commit on this stage's barrier not yet waited for (same in every thread)
+#pragma unroll
+    for (int st = 0; st < kStages; ++st) {
+        phase[st] = 0u;
+        pending[st] = 0;
+    }
+    auto a_tile = [&](int st) { return smem + st * kStageBytes; };                        // 128 x 32 bf16 = 8 KB
+    auto b_tile = [&](int st) { return smem + st * kStageBytes + kTileM * kChunkK * 2; };  // N x 32 bf16 <= 16 KB
+    // the first kAhead chunks, one cp.async group each
+    for (int c = 0; c < kAhead; ++c) {
+        if (c < chunks) {
+            stage_async(a_tile(c), A, K, m0, kTileM, M, c * kChunkK);
+            stage_async(b_tile(c), B, K, 0, N, N, c * kChunkK);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     bool ok = true;
     for (int c = 0; c < chunks; ++c) {
-        const int st = c & 1;
-        uint8_t* a_tile = smem + st * kStageBytes;           // 128 x 32 bf16 = 8 KB
-        uint8_t* b_tile = a_tile + kTileM * kChunkK * 2;      // N x 32 bf16 <= 16 KB
-        if (pending[st]) {
-            const bool arrived = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]);
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            ok = __syncthreads_and(arrived) != 0;  // the same decision in every thread
-            if (!ok) break;
-            phase[st] ^= 1u;
-            pending[st] = 0;
+        // refill the stage of chunk c + kAhead, last read by the MMAs of chunk c + kAhead - kStages
+        const int next = c + kAhead, sn = next % kStages;
+        if (next < chunks) {
+            if (pending[sn]) {
+                const bool arrived = mbar_wait_bounded(smem_u32(&bar[sn]), phase[sn], g_loop_wait_limit);
+                ok = __syncthreads_and(arrived) != 0;  // the same decision in every thread
+                if (!ok) break;
+                phase[sn] ^= 1u;
+                pending[sn] = 0;
+            }
+            stage_async(a_tile(sn), A, K, m0, kTileM, M, next * kChunkK);
+            stage_async(b_tile(sn), B, K, 0, N, N, next * kChunkK);
         }
-        stage(a_tile, A, K, m0, kTileM, M, c * kChunkK);
-        stage(b_tile, B, K, 0, N, N, c * kChunkK);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        // chunk c's group has landed once at most kAhead later groups are outstanding
+        asm volatile("cp.async.wait_group %0;" ::"n"(kAhead) : "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        const int st = c % kStages;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
             for (int kk = 0; kk < kChunkK; kk += 16) {
                 // two core matrices along K per MMA: the K-step is 2 x 128 bytes
-                const uint64_t ad = smem_desc(smem_u32(a_tile) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
-                const uint64_t bd = smem_desc(smem_u32(b_tile) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
+                const uint64_t ad = smem_desc(smem_u32(a_tile(st)) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
+                const uint64_t bd = smem_desc(smem_u32(b_tile(st)) + (kk / 8) * kCoreBytes, kCoreBytes, kChunkRowGroupBytes);
                 const uint32_t accumulate = (c * kChunkK + kk) > 0 ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
@@ -149,11 +176,12 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
         }
         pending[st] = 1;
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     // Drain the commits not yet waited for (also after a timeout: every MMA
     // in flight gets a bounded wait before its tensor memory is freed).
     bool drained = true;
 #pragma unroll
-    for (int st = 0; st < 2; ++st)
+    for (int st = 0; st < kStages; ++st)
         if (pending[st]) drained = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]) && drained;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     drained = __syncthreads_and(drained) != 0;
@@ -162,8 +190,10 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
         // tensor memory is freed with MMAs possibly still in flight
         if (threadIdx.x == 0) atomicMax(status, drained ? 1 : 2);
     } else {
-        // epilogue: warp w reads rows 32 w + lane, 32 columns at a time
-        const int row = m0 + 32 * warp + lane;
+        // epilogue: warp w reads rows 32 w + lane, 32 columns at a time, and
+        // writes them back row by row through a padded 32 x 33 block of the
+        // (now idle) operand stages
+        float* block = reinterpret_cast<float*>(smem) + warp * (32 * 33);
         for (int c0 = 0; c0 < N; c0 += 32) {
             uint32_t r[32];
             const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
@@ -178,15 +208,23 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < M) {
-                for (int j = 0; j < 32 && c0 + j < N; ++j) {
-                    float v = __uint_as_float(r[j]);
-                    if (bias) v = v + bias[c0 + j];
-                    if (relu) v = fmaxf(v, 0.0f);
-                    if (D) D[(int64_t)row * N + c0 + j] = v;
-                    if (Dh) Dh[(int64_t)row * N + c0 + j] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+#pragma unroll
+            for (int j = 0; j < 32; ++j) block[lane * 33 + j] = __uint_as_float(r[j]);
+            __syncwarp();
+            const int col = c0 + lane;
+            const float b = (bias && col < N) ? bias[col] : 0.0f;
+            for (int rr = 0; rr < 32; ++rr) {
+                const int row = m0 + 32 * warp + rr;
+                if (row >= M) break;
+                float v = block[rr * 33 + lane];
+                if (bias) v = v + b;
+                if (relu) v = fmaxf(v, 0.0f);
+                if (col < N) {
+                    if (D) D[(int64_t)row * N + col] = v;
+                    if (Dh) Dh[(int64_t)row * N + col] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
                 }
             }
+            __syncwarp();
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -361,6 +399,13 @@ int bm_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* w_bf16, 
     bm::k_adam<<<bm::grid_for(count) < 1216 ? bm::grid_for(count) : 1216, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
         w, g, m, v, w_bf16, count, lr, beta1, beta2, eps, c1, c2);
     return bm::check_cuda("mlp_adam");
+}
+
+int bm_gemm_set_loop_wait_limit(long long limit) {
+    const long long value = limit < 0 ? bm::kWaitLimit : limit;
+    if (cudaMemcpyToSymbol(bm::g_loop_wait_limit, &value, sizeof(value)) != cudaSuccess)
+        return bm::check_cuda("gemm wait limit");
+    return BM_OK;
 }
 
 int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, const float* bias, int relu,

@@ -58,3 +58,36 @@ def test_gemm_bias_relu_and_bf16_copy():
     expected = np.maximum(a @ b.T + bias, 0.0)
     np.testing.assert_allclose(D, expected, rtol=1e-5, atol=1e-4 * np.sqrt(K))
     np.testing.assert_array_equal(Dh, bf16(D)[0])
+
+
+def test_gemm_wait_timeout_reports_status_and_returns():
+    """The bounded-wait path: with the K loop's poll limit at 0 the first wait
+    for a stage (chunk 4 of 8 reuses chunk 0's stage) gives up at once; the
+    kernel drains the MMAs in flight with the full limit, records status 1,
+    writes nothing and returns.  The default limit then computes normally."""
+    import torch
+
+    rng = np.random.default_rng(3)
+    M, N, K = 128, 64, 256
+    a_bits, a = bf16(rng.normal(size=(M, K)))
+    b_bits, b = bf16(rng.normal(size=(N, K)))
+    dev = "cuda:0"
+    A = torch.as_tensor(a_bits.view(np.int16), device=dev)
+    B = torch.as_tensor(b_bits.view(np.int16), device=dev)
+    D = torch.zeros(M, N, dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = _native.lib()
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    _native.check(lib.bm_gemm_set_loop_wait_limit(0))
+    try:
+        _native.check(lib.bm_gemm_tn_bf16(p(A), p(B), p(D), M, N, K, None, 0, None, p(status), None))
+        torch.cuda.synchronize()
+    finally:
+        _native.check(lib.bm_gemm_set_loop_wait_limit(-1))
+    assert status.item() == 1
+    assert not D.any()
+    status.zero_()
+    _native.check(lib.bm_gemm_tn_bf16(p(A), p(B), p(D), M, N, K, None, 0, None, p(status), None))
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    np.testing.assert_allclose(D.cpu().numpy(), a @ b.T, rtol=1e-5, atol=1e-4 * np.sqrt(K))

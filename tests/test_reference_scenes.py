@@ -455,8 +455,10 @@ def set_single_field(c, enabled):
 HALVES = Config(size=(0.06, 0.03, 0.03), grid_spacing=0.0075, dt=0.0005)
 
 
-def pushed_halves(single_field, steps=40):
-    """test_single_field.py:7-18: the left half (code 1) pushed at -0.2 m/s against the right (code 2)."""
+def pushed_halves(single_field, steps=40, arrays=False):
+    """test_single_field.py:7-18: the left half (code 1) pushed at -0.2 m/s against the right (code 2).
+
+    Returns the mean x velocity of each half and the codes, or with arrays=True the oracle itself."""
     c = OracleSolver(HALVES)
     left = c.reference[:, 0] < 0
     c.set("codes", np.where(left, 1, 2).astype(np.int64))
@@ -466,6 +468,8 @@ def pushed_halves(single_field, steps=40):
     set_single_field(c, single_field)
     for _ in range(steps):
         c.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
+    if arrays:
+        return c
     v = c.get("v")
     return v[~left, 0].mean(), v[left, 0].mean(), c.get("codes")
 
@@ -598,9 +602,9 @@ def test_single_field_halves_on_cuda_match_the_oracle():
         g.set_single_field(single)
         for _ in range(40):
             g.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
-        right_v, left_v, codes = pushed_halves(single)
-        np.testing.assert_array_equal(g.v.numpy()[~left, 0].mean(), right_v)
-        np.testing.assert_array_equal(g.codes.numpy(), codes)
+        o = pushed_halves(single, arrays=True)
+        for name in ("x", "v", "F", "stress", "codes"):
+            np.testing.assert_array_equal(getattr(g, name).numpy(), o.get(name), err_msg=f"{name} single={single}")
 
 
 @pytest.mark.gpu
