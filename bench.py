@@ -489,6 +489,52 @@ def run_triple_cut(args, rank, world):
 MLS_BYTES = (276, 56)
 
 
+def run_gemm(args, rank, world):
+    """The predictor's tensor-core GEMM alone (bm_gemm_tn_bf16: bf16 operands, fp32 result) at its
+    hidden-layer shape (N = K = 256) over large row counts, CUDA events on the launching stream."""
+    import torch
+
+    from blademaster_gb300 import _native, replicas
+
+    dist, rank, world, local = replicas.init()
+    torch.cuda.set_device(local)
+    lib = _native.lib()
+    peak_tf = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    status = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
+    shapes = {}
+    for rows in (4096, 32768, 131072):
+        a = torch.randn(rows, 256, device=f"cuda:{local}").to(torch.bfloat16).view(torch.int16)
+        b = torch.randn(256, 256, device=f"cuda:{local}").to(torch.bfloat16).view(torch.int16)
+        d = torch.empty(rows, 256, dtype=torch.float32, device=f"cuda:{local}")
+        call = lambda: _native.check(lib.bm_gemm_tn_bf16(p(a), p(b), p(d), rows, 256, 256, None, 0, None, p(status),
+                                                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        for _ in range(max(args.warmup, 3)):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) / args.steps * 1e3
+        tflops = 2 * rows * 256 * 256 / (us * 1e-6) / 1e12
+        shapes[f"{rows}x256x256"] = {"us": us, "tflops": tflops, "frac_of_bf16_burst": tflops / peak_tf}
+    big = shapes["131072x256x256"]
+    if rank == 0:
+        print(json.dumps({
+            "metric": "bm_gemm_tn_bf16 TFLOP/s (predictor hidden layer)", "value": big["tflops"], "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": big["us"] / 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic", "config": {"workload": "gemm_tn_bf16", "shapes": shapes, "status": int(status.item())},
+            "roofline": {"bound": "tensor", "achieved": big["tflops"], "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": big["frac_of_bf16_burst"], "peak_kind": "of measured bf16 burst"},
+        }), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_mls(args, rank, world):
     """The MLS-MPM baseline step at the block's scale (1.6 M particles, 2 mm grid, dt 10 us): one held
     knife 1 mm into the top face, one 1 ms interval (100 substeps) per step, replayed as one graph."""
@@ -633,6 +679,9 @@ def main():
         return
     if args.workload == "mls_block_1p6M":
         run_mls(args, rank, world)
+        return
+    if args.workload == "gemm_tn_bf16":
+        run_gemm(args, rank, world)
         return
     if args.profile_window >= 0:
         run_profile_window(args)

@@ -16,7 +16,7 @@
 // flight also runs out), frees its tensor memory and returns.  The epilogue
 // reads the accumulator with tcgen05.ld (warp w owns rows 32 w .. 32 w + 31)
 // and transposes each 32 x 32 block through shared memory, so that every
-// store of D writes 32 consecutive columns of one row.
+// store of D writes four rows' 32 consecutive columns, 16 bytes per lane.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -75,20 +75,46 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, 
     return false;
 }
 
-// Stage rows [row0, row0 + rows) x columns [k0, k0 + 32) of a K-major bf16
-// matrix (row stride ld elements) into the core-matrix layout at dst with
-// cp.async, 16 bytes per instruction straight into shared memory; rows
-// beyond `valid` are zero-filled (source size 0, from the matrix's first
-// row, which is always a valid address).
-__device__ __forceinline__ void stage_async(uint8_t* dst, const uint16_t* __restrict__ src, int ld, int row0, int rows,
-                                            int valid, int k0) {
-    for (int t = threadIdx.x; t < rows * (kChunkK / 8); t += blockDim.x) {
-        const int r = t >> 2, piece = t & 3;
-        const bool in = row0 + r < valid;
-        const uint16_t* from = in ? src + (int64_t)(row0 + r) * ld + k0 + 8 * piece : src;
-        const uint32_t to = smem_u32(dst + (r >> 3) * kChunkRowGroupBytes + piece * kCoreBytes + (r & 7) * 16);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(to), "l"(from), "r"(in ? 16 : 0) : "memory");
+// Copies of one K chunk into the core-matrix layout with cp.async, 16 bytes
+// per instruction straight into shared memory.  With 128 threads, thread t
+// copies piece t % 4 (8 elements along K) of rows t / 4 + 32 i: its source
+// and destination advance by fixed steps, so they are set up once per tile.
+// Rows of A beyond M are zero-filled (source size 0, from A itself, which is
+// always a valid address); rows of B beyond N are not copied.
+__device__ __forceinline__ void cp_async16(uint32_t to, const void* from, bool in) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(to), "l"(from), "r"(in ? 16 : 0) : "memory");
+}
+struct ChunkCopy {
+    const uint16_t* a_src;  // row m0 + t / 4, piece t % 4, chunk 0
+    const uint16_t* b_src;  // row t / 4, piece t % 4, chunk 0
+    uint32_t dst;           // offset of (row t / 4, piece t % 4) in a tile
+    int a_rows;             // rows of A this thread copies that lie inside M (0..4)
+    int b_rows;             // rows of B this thread copies (0..8)
+};
+__device__ __forceinline__ ChunkCopy chunk_copy(const uint16_t* A, const uint16_t* B, int M, int N, int K, int m0) {
+    const int r0 = threadIdx.x >> 2, piece = threadIdx.x & 3;
+    ChunkCopy c;
+    c.a_src = A + (int64_t)(m0 + r0) * K + 8 * piece;
+    c.b_src = B + (int64_t)r0 * K + 8 * piece;
+    c.dst = (uint32_t)((r0 >> 3) * kChunkRowGroupBytes + piece * kCoreBytes + (r0 & 7) * 16);
+    c.a_rows = 0;
+    for (int i = 0; i < 4; ++i) c.a_rows += (m0 + r0 + 32 * i < M) ? 1 : 0;
+    c.b_rows = 0;
+    for (int i = 0; i < 8; ++i) c.b_rows += (r0 + 32 * i < N) ? 1 : 0;
+    return c;
+}
+// rows r0 + 32 i are 4 row groups apart in the tile
+constexpr uint32_t kRowStep = 4 * kChunkRowGroupBytes;
+__device__ __forceinline__ void copy_chunk(const ChunkCopy& c, const uint16_t* A, uint32_t a_tile, uint32_t b_tile, int K,
+                                           int k0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool in = i < c.a_rows;
+        cp_async16(a_tile + c.dst + i * kRowStep, in ? c.a_src + (int64_t)i * 32 * K + k0 : A, in);
     }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        if (i < c.b_rows) cp_async16(b_tile + c.dst + i * kRowStep, c.b_src + (int64_t)i * 32 * K + k0, true);
 }
 
 __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B,
@@ -126,12 +152,10 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
     }
     auto a_tile = [&](int st) { return smem + st * kStageBytes; };                        // 128 x 32 bf16 = 8 KB
     auto b_tile = [&](int st) { return smem + st * kStageBytes + kTileM * kChunkK * 2; };  // N x 32 bf16 <= 16 KB
+    const ChunkCopy cc = chunk_copy(A, B, M, N, K, m0);
     // the first kAhead chunks, one cp.async group each
     for (int c = 0; c < kAhead; ++c) {
-        if (c < chunks) {
-            stage_async(a_tile(c), A, K, m0, kTileM, M, c * kChunkK);
-            stage_async(b_tile(c), B, K, 0, N, N, c * kChunkK);
-        }
+        if (c < chunks) copy_chunk(cc, A, smem_u32(a_tile(c)), smem_u32(b_tile(c)), K, c * kChunkK);
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
     bool ok = true;
@@ -140,14 +164,15 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
         const int next = c + kAhead, sn = next % kStages;
         if (next < chunks) {
             if (pending[sn]) {
-                const bool arrived = mbar_wait_bounded(smem_u32(&bar[sn]), phase[sn], g_loop_wait_limit);
+                // one thread polls; the barrier orders its observation before every thread's copies
+                bool arrived = true;
+                if (threadIdx.x == 0) arrived = mbar_wait_bounded(smem_u32(&bar[sn]), phase[sn], g_loop_wait_limit);
                 ok = __syncthreads_and(arrived) != 0;  // the same decision in every thread
                 if (!ok) break;
                 phase[sn] ^= 1u;
                 pending[sn] = 0;
             }
-            stage_async(a_tile(sn), A, K, m0, kTileM, M, next * kChunkK);
-            stage_async(b_tile(sn), B, K, 0, N, N, next * kChunkK);
+            copy_chunk(cc, A, smem_u32(a_tile(sn)), smem_u32(b_tile(sn)), K, next * kChunkK);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
         // chunk c's group has landed once at most kAhead later groups are outstanding
@@ -180,20 +205,26 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
     // Drain the commits not yet waited for (also after a timeout: every MMA
     // in flight gets a bounded wait before its tensor memory is freed).
     bool drained = true;
+    if (threadIdx.x == 0) {
 #pragma unroll
-    for (int st = 0; st < kStages; ++st)
-        if (pending[st]) drained = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]) && drained;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int st = 0; st < kStages; ++st)
+            if (pending[st]) drained = mbar_wait_bounded(smem_u32(&bar[st]), phase[st]) && drained;
+    }
     drained = __syncthreads_and(drained) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok || !drained) {
         // status 1: a wait ran out; 2: the last wait ran out too, so the
         // tensor memory is freed with MMAs possibly still in flight
         if (threadIdx.x == 0) atomicMax(status, drained ? 1 : 2);
     } else {
         // epilogue: warp w reads rows 32 w + lane, 32 columns at a time, and
-        // writes them back row by row through a padded 32 x 33 block of the
-        // (now idle) operand stages
+        // writes them back through a padded 32 x 33 block of the (now idle)
+        // operand stages: lane (r0, q) = (lane / 8, lane % 8) then stores
+        // columns 4 q .. 4 q + 3 of rows r0, r0 + 4, ..., r0 + 28 as one
+        // 16-byte store each (N is a multiple of 16, so a lane's four columns
+        // are all inside D or all outside it)
         float* block = reinterpret_cast<float*>(smem) + warp * (32 * 33);
+        const int q = lane & 7, r0 = lane >> 3;
         for (int c0 = 0; c0 < N; c0 += 32) {
             uint32_t r[32];
             const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
@@ -211,17 +242,33 @@ __global__ void __launch_bounds__(128) k_gemm_tn(const uint16_t* __restrict__ A,
 #pragma unroll
             for (int j = 0; j < 32; ++j) block[lane * 33 + j] = __uint_as_float(r[j]);
             __syncwarp();
-            const int col = c0 + lane;
-            const float b = (bias && col < N) ? bias[col] : 0.0f;
-            for (int rr = 0; rr < 32; ++rr) {
-                const int row = m0 + 32 * warp + rr;
-                if (row >= M) break;
-                float v = block[rr * 33 + lane];
-                if (bias) v = v + b;
-                if (relu) v = fmaxf(v, 0.0f);
-                if (col < N) {
-                    if (D) D[(int64_t)row * N + col] = v;
-                    if (Dh) Dh[(int64_t)row * N + col] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+            const int col = c0 + 4 * q;
+            if (col < N) {
+                float b[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (bias) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) b[e] = bias[col + e];
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int rl = r0 + 4 * i, row = m0 + 32 * warp + rl;
+                    if (row >= M) break;
+                    float v[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        v[e] = block[rl * 33 + 4 * q + e];
+                        if (bias) v[e] = v[e] + b[e];
+                        if (relu) v[e] = fmaxf(v[e], 0.0f);
+                    }
+                    const int64_t at = (int64_t)row * N + col;
+                    if (D) *reinterpret_cast<float4*>(D + at) = make_float4(v[0], v[1], v[2], v[3]);
+                    if (Dh) {
+                        const uint32_t lo = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[0])) |
+                                            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[1])) << 16);
+                        const uint32_t hi = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2])) |
+                                            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[3])) << 16);
+                        *reinterpret_cast<uint2*>(Dh + at) = make_uint2(lo, hi);
+                    }
                 }
             }
             __syncwarp();
@@ -413,6 +460,10 @@ int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N
     if (!A || !B || !status || (!D && !D_bf16)) return bm::fail(BM_ERR_ARGUMENT, "null argument");
     if (M < 1 || N < 16 || N > 256 || N % 16 != 0 || K < 32 || K % 32 != 0)
         return bm::fail(BM_ERR_ARGUMENT, "gemm: need M >= 1, N in 16..256 (multiple of 16), K a multiple of 32");
+    // 16-byte operand copies and 16-byte (fp32) / 8-byte (bf16) result stores
+    if (reinterpret_cast<uintptr_t>(A) % 16 || reinterpret_cast<uintptr_t>(B) % 16 ||
+        reinterpret_cast<uintptr_t>(D) % 16 || reinterpret_cast<uintptr_t>(D_bf16) % 8)
+        return bm::fail(BM_ERR_ARGUMENT, "gemm: A, B and D must be 16-byte aligned, D_bf16 8-byte aligned");
     const unsigned grid = (unsigned)((M + bm::kTileM - 1) / bm::kTileM);
     // 96 KB per CTA keeps at most two CTAs on an SM, so their tensor-memory
     // allocations (at most 256 columns each) always fit the SM's 512 columns.

@@ -524,7 +524,8 @@ int bm_gemm_set_loop_wait_limit(long long limit);
 /* D[M x N] = A[M x K] * B[N x K]^T on the tensor cores (tcgen05): A and B
  * bf16, row-major (K contiguous), fp32 accumulation, then + bias[N] and ReLU
  * if requested; D (fp32) and/or D_bf16 receive the result.  N in 16..256 (a
- * multiple of 16), K a multiple of 32, all rows 16-byte aligned.  *status is
+ * multiple of 16), K a multiple of 32, A, B and D 16-byte aligned, D_bf16
+ * 8-byte aligned (BM_ERR_ARGUMENT otherwise).  *status is
  * set to 1 if the tensor-core work did not complete in time. */
 int bm_gemm_tn_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, const float* bias, int relu,
                     uint16_t* D_bf16, int32_t* status, void* stream);
