@@ -43,6 +43,13 @@ typedef struct { double x, y, z, w; } bm_qd;
 
 /* ------------------------------------------------------------------ bits */
 
+#ifdef ORC_REAL64
+/* The oracle's float64 error-reference build (host C only): `float` is
+ * defined as double there, orc_f32 is the real float32 type, and float bit
+ * patterns (kept in int flag words) are those of the value rounded to float32. */
+BM_HD uint32_t bm_f2u(double f) { union { orc_f32 f; uint32_t u; } c; c.f = (orc_f32)f; return c.u; }
+BM_HD double bm_u2f(uint32_t u) { union { orc_f32 f; uint32_t u; } c; c.u = u; return (double)c.f; }
+#else
 BM_HD uint32_t bm_f2u(float f) {
 #ifdef __CUDA_ARCH__
     return __float_as_uint(f);
@@ -57,6 +64,7 @@ BM_HD float bm_u2f(uint32_t u) {
     union { float f; uint32_t u; } c; c.u = u; return c.f;
 #endif
 }
+#endif
 BM_HD uint64_t bm_d2u(double f) {
 #ifdef __CUDA_ARCH__
     return (uint64_t)__double_as_longlong(f);
@@ -64,7 +72,11 @@ BM_HD uint64_t bm_d2u(double f) {
     union { double f; uint64_t u; } c; c.f = f; return c.u;
 #endif
 }
+#ifdef ORC_REAL64
+BM_HD int bm_isfinitef(double f) { return isfinite(f) != 0; }
+#else
 BM_HD int bm_isfinitef(float f) { return (bm_f2u(f) & 0x7f800000u) != 0x7f800000u; }
+#endif
 BM_HD int bm_isfinite(double f) { return (bm_d2u(f) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull; }
 BM_HD float bm_minf(float a, float b) { return a < b ? a : b; }
 BM_HD float bm_maxf(float a, float b) { return a > b ? a : b; }
@@ -232,6 +244,12 @@ BM_HD bm_v3d qd_rotate_inv(bm_qd q, bm_v3d v) {
 #define BM_LN2_HI_F 0.693145751953125f
 #define BM_LN2_LO_F 1.428606765330187e-06f
 
+#ifdef ORC_REAL64
+/* float64 error-reference build: the C library's double functions */
+BM_HD double bm_logf(double x) { return log(x); }
+BM_HD double bm_expf(double x) { return exp(x); }
+BM_HD double bm_expm1f(double x) { return expm1(x); }
+#else
 BM_HD float bm_logf(float x) {
     uint32_t bits;
     int e;
@@ -280,6 +298,7 @@ BM_HD float bm_expm1f(float x) {
     if (fabsf(x) < 1.0e-3f) return x * (1.0f + 0.5f * x * (1.0f + x / 3.0f));
     return bm_expf(x) - 1.0f;
 }
+#endif
 
 /* ------------------------------------------------ double transcendentals */
 
@@ -502,6 +521,26 @@ BM_HD bm_fx bm_fx_add(bm_fx a, bm_fx b) {
  * from the float's bits so that CPU and GPU agree; |result| saturates at
  * 2^62 and non-finite f gives 0.  Sums of such values are exact and do not
  * depend on their order. */
+#ifdef ORC_REAL64
+/* float64 error-reference build: f * 2^k rounded to the nearest integer,
+ * f * 2^-96 split exactly into the two 64-bit words (truncated below 2^-96). */
+BM_HD int64_t bm_fixed64(double f, int k) {
+    if (!isfinite(f)) return 0;
+    return (int64_t)llround(ldexp(f, k));
+}
+BM_HD double bm_unfixed64(int64_t v, int k) { return ldexp((double)v, -k); }
+BM_HD bm_fx bm_fx_from_float(double f) {
+    bm_fx r;
+    double top, rest;
+    r.lo = 0u; r.hi = 0u;
+    if (!isfinite(f) || fabs(f) >= 2147483648.0) return r;
+    top = floor(ldexp(f, 32));           /* the integer part of f * 2^32 */
+    rest = ldexp(f, 32) - top;           /* in [0, 1), exact */
+    r.hi = (uint64_t)(int64_t)top;
+    r.lo = (uint64_t)ldexp(rest, 64);
+    return r;
+}
+#else
 BM_HD int64_t bm_fixed64(float f, int k) {
     uint32_t bits = bm_f2u(f);
     int exponent = (int)((bits >> 23) & 0xffu), shift;
@@ -549,6 +588,7 @@ BM_HD bm_fx bm_fx_from_float(float f) {
     if (bits >> 31) r = bm_fx_neg(r);
     return r;
 }
+#endif
 BM_HD double bm_fx_to_double(bm_fx a) {
     int negative = (a.hi >> 63) != 0u;
     double v;

@@ -35,6 +35,21 @@
 #include <omp.h>
 #endif
 #include "../include/blademaster_gb300.h"
+#ifdef ORC_REAL64
+/* The float64 error-reference build of this restatement (liboracle64.so):
+ * every float of the restatement and of the shared scalar header becomes
+ * double (the parameter struct above keeps its float32 fields, read as
+ * float32 values), and the float32 libm calls their double counterparts.
+ * It runs the same scenes in double precision so that the float32 results
+ * can be given an error against it; it is never compared bit for bit. */
+typedef float orc_f32;
+#define float double
+#define sqrtf sqrt
+#define fabsf fabs
+#define floorf floor
+#define rintf rint
+#define ldexpf ldexp
+#endif
 #include "../blademaster-lab_gb300/csrc/bm_scalar.h"
 
 #define ORC_API __attribute__((visibility("default")))
@@ -1009,7 +1024,8 @@ static bm_v3 blade_at(const bm_params* P, orc_state* S, int64_t p, int k, tool_f
     } else {
         bm_v3 local = q_rotate_inv(T.rot, v3_sub(xp, T.pos)), closest_local, normal_local, lever, n, relative;
         float distance, front;
-        blade_query(local, P->half, P->bevel, &closest_local, &normal_local, &distance);
+        const float half[3] = {P->half[0], P->half[1], P->half[2]};  /* the working type's copy */
+        blade_query(local, half, P->bevel, &closest_local, &normal_local, &distance);
         front = -P->half[2] - local.z;
         if ((cutting & BM_CUT_HOLD) != 0 && *damage < 1.0f && fabsf(local.x) <= P->half[0] + P->blade_offset &&
             fabsf(local.y) <= P->half[1] && front >= 0.0f) {
@@ -1031,7 +1047,7 @@ static bm_v3 blade_at(const bm_params* P, orc_state* S, int64_t p, int k, tool_f
             hist[0] = h.x; hist[1] = h.y; hist[2] = h.z;
             if (v3_len_sq(j) > 0.0f) {
                 if (cutting != 0)
-                    j = resist_cut(j, xp, vp, T.pos, T.vel, T.rot, T.omega, P->half, P->blade_offset, P->spacing,
+                    j = resist_cut(j, xp, vp, T.pos, T.vel, T.rot, T.omega, half, P->blade_offset, P->spacing,
                                    damage, P->threshold, cutting, &sums->work);
                 result = j;
                 sums_add3(sums->reaction[k], v3_neg(j));

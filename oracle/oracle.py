@@ -33,25 +33,30 @@ from blademaster_gb300.geometry import points, stencil, cell_sort  # noqa: E402
 HERE = Path(__file__).resolve().parent
 SOURCE = HERE / "oracle.c"
 LIBRARY = HERE / "_build" / "liboracle.so"
+# The same restatement built in float64 (-DORC_REAL64): the error reference of scene-level results.
+LIBRARY64 = HERE / "_build" / "liboracle64.so"
 _lock = threading.Lock()
 _lib = None
+_lib64 = None
 
 
-def build(force=False):
-    """Compile the oracle (portable flags: it runs on x86_64 and aarch64)."""
+def build(force=False, real64=False):
+    """Compile the oracle (portable flags: it runs on x86_64 and aarch64); real64 builds the float64 one."""
+    target = LIBRARY64 if real64 else LIBRARY
     with _lock:
         deps = [SOURCE, ROOT / "blademaster-lab_gb300" / "csrc" / "bm_scalar.h", ROOT / "include" / "blademaster_gb300.h"]
-        if not force and LIBRARY.exists() and all(d.stat().st_mtime <= LIBRARY.stat().st_mtime for d in deps):
-            return LIBRARY
-        LIBRARY.parent.mkdir(exist_ok=True)
-        tmp = LIBRARY.with_suffix(".tmp.so")
+        if not force and target.exists() and all(d.stat().st_mtime <= target.stat().st_mtime for d in deps):
+            return target
+        target.parent.mkdir(exist_ok=True)
+        tmp = target.with_suffix(".tmp.so")
         cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+               *(["-DORC_REAL64", "-Werror=incompatible-pointer-types"] if real64 else []),
                str(SOURCE), "-o", str(tmp), "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("oracle build failed:\n" + r.stderr)
-        os.replace(tmp, LIBRARY)
-        return LIBRARY
+        os.replace(tmp, target)
+        return target
 
 
 P = ctypes.c_void_p
@@ -68,8 +73,24 @@ class State(ctypes.Structure):
     _fields_ = [(name, P) for name in _STATE_FIELDS] + [("capacity", ctypes.c_int64), ("buckets", ctypes.c_int64)]
 
 
-def lib():
-    global _lib
+def lib(real64=False):
+    """The float32 oracle, or with real64 the float64 build (whose float arguments are doubles)."""
+    global _lib, _lib64
+    if real64:
+        if _lib64 is None:
+            build(real64=True)
+            L = ctypes.CDLL(str(LIBRARY64))
+            if L.orc_state_size() != ctypes.sizeof(State):
+                raise RuntimeError("oracle state layout mismatch")
+            pp, ps, vp, i = ctypes.POINTER(_native.Params), ctypes.POINTER(State), ctypes.c_void_p, ctypes.c_int
+            for name, args in {"orc_register": [pp, ps, vp], "orc_refresh_stress": [pp, ps],
+                               "orc_load_external": [pp, ps, vp], "orc_validate_interval": [pp, ps],
+                               "orc_substep": [pp, ps, i, i, vp, i, vp, vp]}.items():
+                getattr(L, name).argtypes = args
+                getattr(L, name).restype = None
+            L.orc_num_threads.restype = ctypes.c_int
+            _lib64 = L
+        return _lib64
     if _lib is None:
         build()
         L = ctypes.CDLL(str(LIBRARY))
@@ -136,11 +157,19 @@ def _pow2_at_least(v):
 
 
 class OracleSolver:
-    """The reference's Solver restated on the CPU (device particle order, AoS arrays)."""
+    """The reference's Solver restated on the CPU (device particle order, AoS arrays).
 
-    def __init__(self, config):
+    real=np.float64 runs the float64 build of the same restatement (every float32 array and
+    operation in double, the parameters the float32 values): the error reference that the
+    float32 results (bit-exact with the GPU) are measured against.  Only the scene-stepping
+    methods (step, advance, external_interval, get, set) are available there."""
+
+    def __init__(self, config, real=np.float32):
         cfg = self.config = config
-        self.L = lib()
+        self.R = R = np.dtype(real).type
+        if R not in (np.float32, np.float64):
+            raise ValueError("real must be float32 or float64")
+        self.L = lib(R is np.float64)
         self.reference, self.origin, cells = points(cfg.size, cfg.grid_spacing, cfg.shape, cfg.sampling_seed)
         n = self.n = len(self.reference)
         nodes, w, g = stencil(self.reference, self.origin, cfg.grid_spacing, cells)
@@ -208,32 +237,32 @@ class OracleSolver:
         self.params = p
         cap = _pow2_at_least(max(16 * n, 16))
         A = self.arrays = {}
-        A["x"] = np.ascontiguousarray(self.reference[order], np.float32)
-        A["v"] = np.zeros((n, 3), np.float32)
+        A["x"] = np.ascontiguousarray(self.reference[order], R)
+        A["v"] = np.zeros((n, 3), R)
         A["ref"] = A["x"].copy()
-        A["F"] = np.tile(np.eye(3, dtype=np.float32).reshape(9), (n, 1))
+        A["F"] = np.tile(np.eye(3, dtype=R).reshape(9), (n, 1))
         A["Fp"] = A["F"].copy()
-        A["stress"] = np.zeros((n, 9), np.float32)
+        A["stress"] = np.zeros((n, 9), R)
         A["viscous"] = np.zeros((n, 9), np.float64)
         A["codes"] = np.zeros(n, np.int64)
         A["zero_codes"] = np.zeros(n, np.int64)
-        A["damage"] = np.zeros((K, n), np.float32)
-        A["histories"] = np.zeros((1 + K, n, 3), np.float32)
-        A["impulses"] = np.zeros((n, 3), np.float32)
+        A["damage"] = np.zeros((K, n), R)
+        A["histories"] = np.zeros((1 + K, n, 3), R)
+        A["impulses"] = np.zeros((n, 3), R)
         A["nodes"] = np.ascontiguousarray(nodes[order], np.int32)
-        A["weights"] = np.ascontiguousarray(w[order], np.float32)
-        A["gradients"] = np.ascontiguousarray(g[order], np.float32)
+        A["weights"] = np.ascontiguousarray(w[order], R)
+        A["gradients"] = np.ascontiguousarray(g[order], R)
         A["keys"] = np.full(cap, -1, np.int64)
         A["slots"] = np.zeros((n, 8), np.int32)
         A["node_start"] = np.zeros(self.node_count + 1, np.int32)
         A["node_slots"] = np.zeros(cap, np.int32)
         A["slot_start"] = np.zeros(cap + 1, np.int32)
         A["contrib"] = np.zeros(8 * n, np.int32)
-        A["grid_mass"] = np.zeros(cap, np.float32)
+        A["grid_mass"] = np.zeros(cap, R)
         for k in ("momentum", "grid_impulse", "old_v", "new_v", "remapped", "coupled"):
-            A[k] = np.zeros((cap, 3), np.float32)
+            A[k] = np.zeros((cap, 3), R)
         A["pair_keys"] = np.full((2, p.pair_capacity), -1, np.int64)
-        A["pair_history"] = np.zeros((2, p.pair_capacity, 3), np.float32)
+        A["pair_history"] = np.zeros((2, p.pair_capacity, 3), R)
         A["pair_used"] = np.zeros((2, p.pair_capacity), np.int32)
         A["pair_count"] = np.zeros(2, np.int32)
         buckets = _pow2_at_least(max(2 * n, 1024))
@@ -241,19 +270,19 @@ class OracleSolver:
         A["cell_next"] = np.zeros(n, np.int32)
         A["cell_start"] = cell_start.astype(np.int32)
         tool = np.zeros((K, 13))
-        tool[:, 2] = np.float32(cfg.size[2] + 0.012 + hz)
+        tool[:, 2] = R(cfg.size[2] + 0.012 + hz)
         tool[:, 9] = 1.0
         A["tool"] = tool
-        A["mobility"] = np.zeros(36, np.float32)
+        A["mobility"] = np.zeros(36, R)
         A["acc"] = np.zeros(_native.ACC_WORDS, np.uint64)
         A["interval"] = np.zeros(6)
         A["table_impulse"] = np.zeros((K, 3))
-        A["speed"] = np.zeros(1, np.float32)
+        A["speed"] = np.zeros(1, R)
         A["errors"] = np.zeros(3, np.int32)
         A["flags"] = np.zeros(_native.FLAG["WORDS"], np.int32)
         A["flags"][_native.FLAG["TOPOLOGY_DIRTY"]] = 1
-        A["result"] = np.zeros(10 + 7 * 4097, np.float32)
-        A["hold_side"] = np.zeros(n, np.float32)
+        A["result"] = np.zeros(10 + 7 * 4097, R)
+        A["hold_side"] = np.zeros(n, R)
         s = State()
         for name in _STATE_FIELDS:
             setattr(s, name, A[name].ctypes.data)
@@ -314,7 +343,7 @@ class OracleSolver:
             A[name][:] = value.reshape(-1, 3)[self.order]
         elif name in ("F", "Fp"):
             A[name][:] = value.reshape(-1, 9)[self.order]
-            if name == "Fp" and not np.all(A["Fp"] == np.eye(3, dtype=np.float32).reshape(9)):
+            if name == "Fp" and not np.all(A["Fp"] == np.eye(3, dtype=self.R).reshape(9)):
                 self.params.use_fp = 1
         elif name == "codes":
             A["codes"][:] = value[self.order]
@@ -330,7 +359,7 @@ class OracleSolver:
         elif name == "tool_omega":
             A["tool"][:, 10:13] = np.asarray(value, np.float32).reshape(-1, 3)
         elif name == "mobility":
-            A["mobility"][:] = np.asarray(value, np.float32).reshape(36)
+            A["mobility"][:] = np.asarray(value, self.R).reshape(36)
         else:
             A[name][...] = value
 
@@ -373,8 +402,8 @@ class OracleSolver:
     def step(self, target_edge=(0.0, 0.0, 0.042), cutting=True, cut_index=0, orientation=None):
         self.set_cut(cut_index)
         self.arrays["flags"][_native.FLAG["STEP"]] = self.step_count
-        target = np.asarray(target_edge, np.float32).reshape(3)
-        rot = np.asarray(orientation if orientation is not None else [0, 0, 0, 1], np.float32).reshape(4)
+        target = np.asarray(target_edge, np.float32).astype(self.R).reshape(3)
+        rot = np.asarray(orientation if orientation is not None else [0, 0, 0, 1], np.float32).astype(self.R).reshape(4)
         self.L.orc_substep(ctypes.byref(self.params), ctypes.byref(self.S), self.cut_bits(cutting), int(cut_index),
                            self._field_codes(), int(self.config.cache_topology), ptr(target), ptr(rot))
         self.step_count += 1
@@ -398,10 +427,10 @@ class OracleSolver:
     def external_interval(self, state_packed, steps, cutting=True, cut_index=0):
         """ExternalToolPort.advance (coupling.py:88-189): returns (impulse, angular about the world origin, errors)."""
         self.set_cut(cut_index)
-        packed = np.asarray(state_packed, np.float32)
+        packed = np.asarray(state_packed, np.float32).astype(self.R)
         self.L.orc_load_external(ctypes.byref(self.params), ctypes.byref(self.S), ptr(packed))
-        dummy_t = np.zeros(3, np.float32)
-        dummy_q = np.array([0, 0, 0, 1], np.float32)
+        dummy_t = np.zeros(3, self.R)
+        dummy_q = np.array([0, 0, 0, 1], self.R)
         for _ in range(steps):
             self.arrays["flags"][_native.FLAG["STEP"]] = self.step_count
             self.L.orc_substep(ctypes.byref(self.params), ctypes.byref(self.S), self.cut_bits(cutting), int(cut_index),

@@ -7,7 +7,9 @@
   the whole simulated second (4000 substeps) bit for bit, with the
   reference's outputs: edge height, directional work, damage count and
   piece count (paper_freefall.py:134-157).  At this stiffness the knife
-  stalls 1.3 mm into the top face and tips over; nothing is severed.
+  stalls 1.3 mm into the top face and tips over; nothing is severed.  (The
+  tip-over is float32 round-off breaking the scene's mirror symmetry: in the
+  oracle's float64 build the knife stays upright; tests/test_fp64_scenes.py.)
 * Triple cut of the Maxwell cylinder through ExternalToolPort (4480
   particles, 1390 coupling intervals of 2 ms): every interval's impulse and
   angular impulse, the final state and the four pieces, bit for bit.
