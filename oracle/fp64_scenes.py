@@ -8,8 +8,8 @@ run's error against the float64 one for the quantities the scenes are judged
 by: the blade's impulse (force times time) and angular impulse per coupling
 interval, the knife's trajectory, cutting work, damage and pieces.
 
-    python oracle/fp64_scenes.py freefall_8960      # C1: the whole simulated second
-    python oracle/fp64_scenes.py triple_cut_4480    # C2: all 1390 port intervals
+    python oracle/fp64_scenes.py freefall_8960      # the gravity knife: the whole simulated second
+    python oracle/fp64_scenes.py triple_cut_4480    # the triple cut: all 1390 port intervals
     python oracle/fp64_scenes.py triple_cut_4480 --intervals 200
 
 Prints one JSON object.  Relative errors of per-interval impulses are taken
@@ -38,7 +38,7 @@ from oracle.oracle import OracleSolver  # noqa: E402
 
 
 def freefall(substeps=4000, window=40):
-    """C1 at the stable step: the knife's reaction impulse per `window` substeps, its pose, work and damage."""
+    """The gravity knife (8960 particles) at the stable step: the knife's reaction impulse per `window` substeps, its pose, work and damage."""
     cfg, pos, _ = scenes.gravity_knife()
     runs = {}
     for real in (np.float32, np.float64):
@@ -80,7 +80,7 @@ def freefall(substeps=4000, window=40):
 
 
 def triple_cut(intervals=None):
-    """C2 through the port: every interval's impulse and angular impulse, final damage and pieces."""
+    """The triple cut of the Maxwell cylinder (4480 particles) through the port: every interval's impulse and angular impulse, final damage and pieces."""
     cfg = scenes.triple_cut_config()
     schedule = scenes.triple_cut_schedule()[:intervals]
     steps = int(round(scenes.TRIPLE_CUT_INTERVAL / cfg.dt))

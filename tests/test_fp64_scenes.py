@@ -4,8 +4,8 @@ The CUDA path reproduces the float32 oracle bit for bit; the oracle's float64
 build (``OracleSolver(cfg, real=np.float64)``) runs the same restatement in
 double precision.  These tests run the leading part of two benchmark scenes
 in both and bound the float32 run's error on what the scenes are judged by:
-the blade's impulse per coupling interval (the benchmark spec's 0.5 % on blade
-force and impulse) and the knife's pose.  ``oracle/fp64_scenes.py`` runs the
+the blade's impulse per coupling interval (blade force and impulse are held
+to 0.5 %) and the knife's pose.  ``oracle/fp64_scenes.py`` runs the
 whole scenes and reports the same errors.
 """
 
@@ -34,7 +34,7 @@ def test_float64_build_runs_the_same_scene():
 
 
 def test_gravity_knife_landing_against_float64():
-    # the first 0.1 s of C1: the knife lands and starts cutting; 10 ms windows of its reaction impulse
+    # the first 0.1 s of the gravity knife (8960 particles): the knife lands and starts cutting; 10 ms windows of its reaction impulse
     r = freefall(substeps=400)
     assert r["interval_error_of_largest"]["max"] < 1e-4
     assert r["total"]["relative_error"] < 1e-5
@@ -44,9 +44,9 @@ def test_gravity_knife_landing_against_float64():
 
 
 def test_triple_cut_first_intervals_against_float64():
-    # the first 60 port intervals of C2: the knife descends through the Maxwell cylinder
+    # the first 60 port intervals of the triple cut (4480 particles): the knife descends through the Maxwell cylinder
     r = triple_cut(intervals=60)
     assert r["largest_interval_impulse"] > 1e-4  # the knife is in contact
     assert r["interval_error_of_largest"]["max"] < 1e-3
-    assert r["total"]["relative_error"] < 5e-3  # the benchmark spec's 0.5 % on the blade impulse
+    assert r["total"]["relative_error"] < 5e-3  # blade impulse within 0.5 %
     assert r["released_particles"]["float32"] == r["released_particles"]["float64"] > 0
