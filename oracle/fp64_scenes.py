@@ -11,6 +11,7 @@ interval, the knife's trajectory, cutting work, damage and pieces.
     python oracle/fp64_scenes.py freefall_8960      # the gravity knife: the whole simulated second
     python oracle/fp64_scenes.py triple_cut_4480    # the triple cut: all 1390 port intervals
     python oracle/fp64_scenes.py triple_cut_4480 --intervals 200
+    python oracle/fp64_scenes.py block_1p6M_8knives --substeps 100   # 1.6 M particles: ~1 s per substep each
 
 Prints one JSON object.  Relative errors of per-interval impulses are taken
 against the largest interval impulse of the float64 run (intervals without
@@ -79,6 +80,46 @@ def freefall(substeps=4000, window=40):
     }
 
 
+def block(substeps=100, window=10):
+    """The 1.6 M-particle block with 8 knives from t = 0: every knife's reaction impulse per `window`
+    substeps, the knives' poses, damage and the particle positions."""
+    cfg, knives, velocity = scenes.block_8knives()
+    runs = {}
+    for real in (np.float32, np.float64):
+        o = OracleSolver(cfg, real=real)
+        o.set("tool_pos", knives)
+        o.set("tool_vel", velocity)
+        impulses, begin = [], time.perf_counter()
+        acc = np.zeros((cfg.tool_count, 3))
+        for i in range(substeps):
+            o.step((0.0, 0.0, 0.0), cutting=True)
+            acc += o.get("reaction")
+            if (i + 1) % window == 0:
+                impulses.append(acc.copy())
+                acc[:] = 0.0
+        runs[real.__name__] = {
+            "impulses": np.array(impulses),  # [windows][knives][3]
+            "tool": o.get("tool").copy(),
+            "released": int(np.count_nonzero(o.get("tool_damage") >= 1.0)),
+            "x": o.get("x").astype(np.float64), "errors": o.get("errors").tolist(),
+            "seconds": time.perf_counter() - begin,
+        }
+    a, b = runs["float32"], runs["float64"]
+    # all knives' windows as one series of 3-vectors
+    per_knife = {f"knife_{k}": impulse_errors(a["impulses"][:, k], b["impulses"][:, k])["total"]["relative_error"]
+                 for k in range(cfg.tool_count)}
+    return {
+        "scene": "block_1p6M_8knives", "substeps": substeps, "window_substeps": window,
+        **impulse_errors(a["impulses"].reshape(-1, 3), b["impulses"].reshape(-1, 3)),
+        "total_relative_error_per_knife": per_knife,
+        "knife_position_difference_m": float(np.abs(a["tool"][:, 0:3] - b["tool"][:, 0:3]).max()),
+        "released_particles": {"float32": a["released"], "float64": b["released"]},
+        "particle_position_difference_m": float(np.abs(a["x"] - b["x"]).max()),
+        "device_errors": {"float32": a["errors"], "float64": b["errors"]},
+        "cpu_seconds": {"float32": a["seconds"], "float64": b["seconds"]},
+    }
+
+
 def triple_cut(intervals=None):
     """The triple cut of the Maxwell cylinder (4480 particles) through the port: every interval's impulse and angular impulse, final damage and pieces."""
     cfg = scenes.triple_cut_config()
@@ -135,11 +176,17 @@ def impulse_errors(f32, f64):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("scene", choices=["freefall_8960", "triple_cut_4480"])
-    ap.add_argument("--substeps", type=int, default=4000, help="freefall_8960: substeps (4000 = 1 s)")
+    ap.add_argument("scene", choices=["freefall_8960", "triple_cut_4480", "block_1p6M_8knives"])
+    ap.add_argument("--substeps", type=int, default=None,
+                    help="freefall_8960: substeps (default 4000 = 1 s); block_1p6M_8knives: substeps (default 100)")
     ap.add_argument("--intervals", type=int, default=None, help="triple_cut_4480: leading port intervals (all 1390)")
     args = ap.parse_args()
-    out = freefall(args.substeps) if args.scene == "freefall_8960" else triple_cut(args.intervals)
+    if args.scene == "freefall_8960":
+        out = freefall(args.substeps or 4000)
+    elif args.scene == "block_1p6M_8knives":
+        out = block(args.substeps or 100)
+    else:
+        out = triple_cut(args.intervals)
     print(json.dumps(out, indent=1))
 
 
