@@ -517,9 +517,10 @@ int bm_mls_graph_create(bm_mls* s, int steps, void* stream, bm_graph** out);
  * linear mobility prediction of tool_substep "predict", tool.py:97-113).
  * ------------------------------------------------------------------------ */
 /* Test hook: the poll limit of bm_gemm_tn_bf16's waits inside its K loop
- * (limit < 0 restores the default).  With 0 the first wait for a stage
- * gives up at once, so a GEMM of K >= 128 records status 1 after draining
- * the MMAs in flight; tests use it to drive the timeout path. */
+ * on the current device (limit < 0 restores the default).  With 0 the first
+ * wait for a stage gives up at once, so a GEMM of K >= 128 records status 1
+ * after draining the MMAs in flight (the drain always waits the full limit);
+ * tests use it to drive the timeout path. */
 int bm_gemm_set_loop_wait_limit(long long limit);
 /* D[M x N] = A[M x K] * B[N x K]^T on the tensor cores (tcgen05): A and B
  * bf16, row-major (K contiguous), fp32 accumulation, then + bias[N] and ReLU
