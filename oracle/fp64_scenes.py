@@ -12,6 +12,7 @@ interval, the knife's trajectory, cutting work, damage and pieces.
     python oracle/fp64_scenes.py triple_cut_4480    # the triple cut: all 1390 port intervals
     python oracle/fp64_scenes.py triple_cut_4480 --intervals 200
     python oracle/fp64_scenes.py block_1p6M_8knives --substeps 100   # 1.6 M particles: ~1 s per substep each
+    python oracle/fp64_scenes.py block_1p6M_8knives --spacing 0.003 --substeps 1200 --perturb 1e-8
 
 Prints one JSON object.  Relative errors of per-interval impulses are taken
 against the largest interval impulse of the float64 run (intervals without
@@ -80,14 +81,18 @@ def freefall(substeps=4000, window=40):
     }
 
 
-def block(substeps=100, window=10):
-    """The 1.6 M-particle block with 8 knives from t = 0: every knife's reaction impulse per `window`
-    substeps, the knives' poses, damage and the particle positions."""
-    cfg, knives, velocity = scenes.block_8knives()
+def block(substeps=100, window=10, spacing=0.002, perturb=0.0):
+    """The block with 8 knives from t = 0 (1.6 M particles at the 2 mm grid): every knife's reaction
+    impulse per `window` substeps, the knives' poses, damage and the particle positions.
+
+    With perturb > 0 the second run is float32 again, its knives started `perturb` metres lower:
+    a measure of how far the scene itself amplifies a tiny difference."""
+    cfg, knives, velocity = scenes.block_8knives(spacing)
     runs = {}
-    for real in (np.float32, np.float64):
+    for label, real, shift in (("float32", np.float32, 0.0),
+                               ("float64", np.float32 if perturb > 0 else np.float64, perturb)):
         o = OracleSolver(cfg, real=real)
-        o.set("tool_pos", knives)
+        o.set("tool_pos", knives - np.array([0.0, 0.0, shift]))
         o.set("tool_vel", velocity)
         impulses, begin = [], time.perf_counter()
         acc = np.zeros((cfg.tool_count, 3))
@@ -97,7 +102,7 @@ def block(substeps=100, window=10):
             if (i + 1) % window == 0:
                 impulses.append(acc.copy())
                 acc[:] = 0.0
-        runs[real.__name__] = {
+        runs[label] = {
             "impulses": np.array(impulses),  # [windows][knives][3]
             "tool": o.get("tool").copy(),
             "released": int(np.count_nonzero(o.get("tool_damage") >= 1.0)),
@@ -109,7 +114,8 @@ def block(substeps=100, window=10):
     per_knife = {f"knife_{k}": impulse_errors(a["impulses"][:, k], b["impulses"][:, k])["total"]["relative_error"]
                  for k in range(cfg.tool_count)}
     return {
-        "scene": "block_1p6M_8knives", "substeps": substeps, "window_substeps": window,
+        "scene": f"block_{o.n}_8knives", "substeps": substeps, "window_substeps": window,
+        "second_run": f"float32, knives {perturb} m lower" if perturb > 0 else "float64",
         **impulse_errors(a["impulses"].reshape(-1, 3), b["impulses"].reshape(-1, 3)),
         "total_relative_error_per_knife": per_knife,
         "knife_position_difference_m": float(np.abs(a["tool"][:, 0:3] - b["tool"][:, 0:3]).max()),
@@ -180,11 +186,14 @@ def main():
     ap.add_argument("--substeps", type=int, default=None,
                     help="freefall_8960: substeps (default 4000 = 1 s); block_1p6M_8knives: substeps (default 100)")
     ap.add_argument("--intervals", type=int, default=None, help="triple_cut_4480: leading port intervals (all 1390)")
+    ap.add_argument("--spacing", type=float, default=0.002, help="block_1p6M_8knives: grid spacing (0.003: 0.47 M)")
+    ap.add_argument("--perturb", type=float, default=0.0,
+                    help="block_1p6M_8knives: compare with float32 again, knives started this much lower (m)")
     args = ap.parse_args()
     if args.scene == "freefall_8960":
         out = freefall(args.substeps or 4000)
     elif args.scene == "block_1p6M_8knives":
-        out = block(args.substeps or 100)
+        out = block(args.substeps or 100, spacing=args.spacing, perturb=args.perturb)
     else:
         out = triple_cut(args.intervals)
     print(json.dumps(out, indent=1))

@@ -88,6 +88,8 @@ def lib(real64=False):
                                "orc_substep": [pp, ps, i, i, vp, i, vp, vp]}.items():
                 getattr(L, name).argtypes = args
                 getattr(L, name).restype = None
+            L.orc_count_embedded.argtypes = [pp, ps]
+            L.orc_count_embedded.restype = ctypes.c_int64
             L.orc_num_threads.restype = ctypes.c_int
             _lib64 = L
         return _lib64
@@ -438,6 +440,10 @@ class OracleSolver:
             self.step_count += 1
         self.L.orc_validate_interval(ctypes.byref(self.params), ctypes.byref(self.S))
         return self.arrays["interval"][:3].copy(), self.arrays["interval"][3:].copy(), self.arrays["errors"].copy()
+
+    def embedded_particles(self):
+        """Solver.embedded_particles (solver.py:892-900): particles beside the blade body, inside the labelling band."""
+        return int(self.L.orc_count_embedded(ctypes.byref(self.params), ctypes.byref(self.S)))
 
     def num_threads(self):
         return self.L.orc_num_threads()

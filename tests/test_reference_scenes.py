@@ -15,6 +15,8 @@ bit-exactly with the oracle on the same inputs:
   (tests/test_stress_replays.py:61-87);
 * a cut at index 25 (digit 3^25, beyond 32 bits) severs the banana into two
   pieces (tests/test_coupling.py:131-145);
+* strokes found from the embedded-particle count label each cut plane with
+  its own digit (tests/test_coupling.py:147-186);
 * several free knives: only free knives may be several, slot order does not
   matter, mirrored knives move alike and label their own digits, a knife
   beside the block falls freely, each knife pays its own cutting work
@@ -309,6 +311,79 @@ def test_cut_index_beyond_32_bit_digits_still_severs():
     assert len(sizes) == 2 and sizes.min() > 0.3 * c.n
 
 
+# ----------------------------------------------------------- auto strokes
+
+class Strokes:
+    """The reference's contact-stroke rule (teleop_input.py:239-266), the caller of the embedded count: a
+    stroke starts when particles are embedded beside the blade and ends once none has been for `clear_s`;
+    the cut index advances as it ends."""
+
+    def __init__(self, clear_s=0.02):
+        self.clear_s, self.cut_index, self.strokes, self.inside, self.out_for = clear_s, 0, 0, False, 0.0
+
+    def update(self, embedded, dt):
+        if embedded:
+            self.strokes += not self.inside
+            self.inside, self.out_for = True, 0.0
+        elif self.inside:
+            self.out_for += dt
+            if self.out_for >= self.clear_s:
+                self.cut_index, self.inside = self.cut_index + 1, False
+        return self.cut_index
+
+
+def stroke_states(half, dt=0.001):
+    """tests/test_coupling.py:154-171: the edge goes down through x = -25 mm, back out, over, down through
+    x = +25 mm and out again; one ToolState per 1 ms interval, with the velocity of its leg."""
+    legs = [(-0.025, 0.0, 0.9), (-0.025, 0.0, 0.1), (-0.025, 0.04, 0.6), (0.025, 0.04, 0.8),
+            (0.025, 0.0, 1.0), (0.025, 0.0, 0.1), (0.025, 0.04, 0.6)]
+    path = [(-0.025, 0.036)]
+    for x, z, seconds in legs:
+        x0, z0 = path[-1]
+        path += [(x0 + (x - x0) * k * dt / seconds, z0 + (z - z0) * k * dt / seconds)
+                 for k in range(1, round(seconds / dt) + 1)]
+    return [ToolState([x1, 0.0, z1 + half], [0, 0, 0, 1], [(x1 - x0) / dt, 0.0, (z1 - z0) / dt], [0, 0, 0])
+            for (x0, z0), (x1, z1) in zip(path, path[1:])]
+
+
+def embedded_bounds(x, tool, spacing, half, margin=1e-6):
+    """contact.count_embedded (contact.py:1042-1055) in float64 numpy: the particles inside the band box
+    by more than `margin` (m), and those inside it or within `margin` of its faces."""
+    qx, qy, qz, qw = tool[6:10] / np.linalg.norm(tool[6:10])
+    R = np.array([[1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)],
+                  [2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)],
+                  [2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)]])
+    local = np.abs((x.astype(np.float64) - tool[0:3]) @ R)  # rows are R^T (x - pos)
+    box = np.array([6.0 * spacing, half[1], half[2]])
+    return int(np.all(local < box - margin, axis=1).sum()), int(np.all(local <= box + margin, axis=1).sum())
+
+
+def test_auto_strokes_label_each_cut_plane_with_its_own_digit():
+    # tests/test_coupling.py:147-186: the embedded-particle count drives the stroke rule; two strokes,
+    # each labelled with its own digit, three pieces, and withdrawing from the first kerf writes no second
+    # digit.  Every interval's count also lies within the float64 count's margin band.
+    from blademaster_gb300.presets import banana_config
+
+    cfg = replace(banana_config(), external_tool=True)
+    c, strokes = OracleSolver(cfg), Strokes()
+    steps, before, inside = round(0.001 / cfg.dt), None, 0
+    for state in stroke_states(cfg.blade_half_size[2]):
+        before = c.get("codes").copy() if strokes.strokes == 1 else before
+        c.external_interval(packed(state), steps, cutting=True, cut_index=strokes.cut_index)
+        n = c.embedded_particles()
+        lo, hi = embedded_bounds(c.get("x"), c.get("tool")[0], cfg.grid_spacing, cfg.blade_half_size)
+        assert lo <= n <= hi
+        inside += n > 0
+        strokes.update(n > 0, 0.001)
+    assert inside > 1000 and n == 0
+    assert strokes.strokes == 2 and strokes.cut_index == 2
+    assert np.all((before // 3) % 3 == 0)
+    codes = c.get("codes")
+    assert np.any((codes // 3) % 3 != 0)
+    _, sizes = components(c.node_numpy, c.weight_numpy, codes)
+    assert len(sizes) == 3
+
+
 # ------------------------------------------------------ several free knives
 
 def two_knives(**kwargs):
@@ -531,6 +606,34 @@ def test_deep_digit_severs_on_cuda_and_matches_the_oracle_first():
     assert set(np.unique(codes // 3**cut)) == {0, 1, 2}
     _, sizes = g.components()
     assert len(sizes) == 2 and sizes.min() > 0.3 * g.n
+
+
+@pytest.mark.gpu
+def test_auto_strokes_on_cuda_match_the_oracle():
+    # test_coupling.py:147-186 on the CUDA solver: every interval's embedded count (Solver.embedded_particles,
+    # solver.py:892-900) equals the oracle's, embedded_particles_previous (solver.py:902-918) lags it by one
+    # call, and the strokes, digits, codes and pieces come out as on the oracle
+    from blademaster_gb300.coupling import ExternalToolPort
+    from blademaster_gb300.presets import banana_config
+    from blademaster_gb300.solver import Solver
+
+    cfg = replace(banana_config(), external_tool=True)
+    g, c = Solver(cfg), OracleSolver(cfg)
+    port, strokes, steps = ExternalToolPort(g), Strokes(), round(0.001 / cfg.dt)
+    counts, previous = [], []
+    for i, state in enumerate(stroke_states(cfg.blade_half_size[2])):
+        port.advance(state, 0.001, cutting=True, cut_index=strokes.cut_index)
+        c.external_interval(packed(state), steps, cutting=True, cut_index=strokes.cut_index)
+        counts.append(g.embedded_particles())
+        assert counts[-1] == c.embedded_particles(), f"interval {i}"
+        previous.append(g.embedded_particles_previous())
+        strokes.update(counts[-1] > 0, 0.001)
+    assert previous[0] == 0 and previous[1:] == counts[:-1]
+    assert strokes.strokes == 2 and strokes.cut_index == 2
+    for name in ("x", "v", "codes", "damage"):
+        np.testing.assert_array_equal(getattr(g, name).numpy(), c.get(name), err_msg=name)
+    _, sizes = g.components()
+    assert len(sizes) == 3
 
 
 def cuda_two_knives(**kwargs):
