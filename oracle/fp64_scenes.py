@@ -4,8 +4,8 @@ Runs a benchmark scene twice on the CPU oracle: the float32 restatement (whose
 results the CUDA path reproduces bit for bit) and its float64 build
 (``OracleSolver(cfg, real=np.float64)``: every float32 array and operation in
 double, float64 stencils and reference positions), and reports the float32
-run's error against the float64 one for the quantities the scenes are judged
-by: the blade's impulse (force times time) and angular impulse per coupling
+run's error against the float64 one for the quantities the scenes report:
+the blade's impulse (force times time) and angular impulse per coupling
 interval, the knife's trajectory, cutting work, damage and pieces.
 
     python oracle/fp64_scenes.py freefall_8960      # the gravity knife: the whole simulated second
