@@ -763,6 +763,11 @@ static void hold_constraint(const bm_params* P, orc_state* S) {
     free(active); free(mark); free(list); free(nodes);
 }
 
+/* BladeConstraint.solve (blade_constraint.py:254-324) alone, on the current
+ * grid velocities and masses, as the reference's tests/test_blade_constraint.py
+ * calls it. */
+ORC_API void orc_hold_solve(const bm_params* P, orc_state* S) { hold_constraint(P, S); }
+
 ORC_API void orc_material_step(const bm_params* P, orc_state* S, const int64_t* field_codes, int register_now) {
     int64_t s, p;
     if (register_now) orc_register(P, S, field_codes);

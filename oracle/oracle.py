@@ -113,6 +113,7 @@ def lib(real64=False):
             "orc_clear_step": [pp, ps],
             "orc_load_external": [pp, ps, vp],
             "orc_validate_interval": [pp, ps],
+            "orc_hold_solve": [pp, ps],
             "orc_substep": [pp, ps, i, i, vp, i, vp, vp],
             "orc_friction": [vp, vp, vp, vp, i, f, f, f, f, f, f, vp, vp],
             "orc_blade_query": [vp, i, vp, f, vp, vp, vp],
@@ -440,6 +441,10 @@ class OracleSolver:
             self.step_count += 1
         self.L.orc_validate_interval(ctypes.byref(self.params), ctypes.byref(self.S))
         return self.arrays["interval"][:3].copy(), self.arrays["interval"][3:].copy(), self.arrays["errors"].copy()
+
+    def hold_solve(self):
+        """BladeConstraint.solve (blade_constraint.py:254-324) alone, on the current grid velocities and masses."""
+        self.L.orc_hold_solve(ctypes.byref(self.params), ctypes.byref(self.S))
 
     def embedded_particles(self):
         """Solver.embedded_particles (solver.py:892-900): particles beside the blade body, inside the labelling band."""

@@ -7,6 +7,11 @@ into that face.  The projected-gradient solve must activate, converge below
 the reference's 1e-6 m/s residual, and keep the interval momentum balance
 (material momentum change + knife impulse = gravity impulse).  On the GPU
 every output must equal the oracle's bit for bit.
+
+The reference's own tests of the solve alone (tests/test_blade_constraint.py:
+no restitution at shared cut fields, the entry side kept across the midplane
+and cleared around the finite edge) run on the oracle with their assertions,
+and on the CUDA solver against the oracle.
 """
 
 from dataclasses import replace
@@ -116,3 +121,216 @@ def test_sweep_instance_that_does_not_converge_fails_like_the_oracle():
                 port.advance(state, 0.001)
     residual = np.int32(o.arrays["flags"][_native.FLAG["HOLD_RESIDUAL"]]).view(np.float32)
     assert s.blade_constraint.max_violation == float(residual) > 1.0e-6
+
+
+# ------------------------------------------- the reference's solve-alone scenes
+
+SMALL = Config(size=(0.012, 0.012, 0.012), grid_spacing=0.006, dt=0.001, external_tool=True)
+
+
+class Held:
+    """The fixture of tests/test_blade_constraint.py:10-54 on the oracle or (cuda) the CUDA solver:
+    64 particles in 2 x 2 x 2 cells, the held knife at the origin and at rest, grid masses and
+    velocities written directly and BladeConstraint.solve() run alone.  The reference puts every
+    stencil on eight shared nodes; here each particle keeps its reference-lattice stencil, which
+    the solve reads the same way (weights and slots do not depend on the current positions)."""
+
+    def __init__(self, cuda=False):
+        self.cuda = cuda
+        if cuda:
+            from blademaster_gb300.solver import Solver
+
+            self.s = Solver(SMALL)
+        else:
+            self.s = OracleSolver(SMALL)
+        self.n = self.s.n
+        self.mass = float(F32(self.s.mass))
+        self.tool(vel=[0, 0, 0], omega=[0, 0, 0], mobility=np.zeros((6, 6)))
+
+    def tool(self, vel, omega, mobility):
+        s = self.s
+        if self.cuda:
+            s.tool_pos.zero_()
+            s.tool_vel.assign([vel])
+            s.tool_omega.assign([omega])
+            s.tool_mobility.assign(np.asarray(mobility, F32))
+        else:
+            s.set("tool_pos", [0.0, 0.0, 0.0])
+            s.set("tool_vel", vel)
+            s.set("tool_omega", omega)
+            s.set("mobility", np.asarray(mobility, F32))
+
+    def held_state(self):
+        if self.cuda:
+            return {k: getattr(self.s, k).numpy().copy() for k in ("tool_pos", "tool_rot", "tool_vel", "tool_omega", "tool_mobility")}
+        return {"tool": self.s.arrays["tool"].copy(), "mobility": self.s.arrays["mobility"].copy()}
+
+    def shared_grid(self, codes):
+        """test_blade_constraint.py:30-43: register the codes, grid masses from the stencils."""
+        s = self.s
+        if self.cuda:
+            s.codes.assign(np.asarray(codes, np.int64))
+            s._register_topology()
+            self.slots, weights, cap = s.slots.numpy(), s.weights.numpy(), s.grid_capacity
+        else:
+            s.set("codes", np.asarray(codes, np.int64))
+            s.register()
+            self.slots, weights, cap = s.arrays["slots"][s.rank], s.arrays["weights"][s.rank], len(s.arrays["grid_mass"])
+        self.weights = weights.astype(np.float64)
+        masses = np.zeros(cap)
+        np.add.at(masses, self.slots.ravel(), (self.mass * self.weights).ravel())
+        if self.cuda:
+            s.grid_mass.assign(masses.astype(F32))
+        else:
+            s.arrays["grid_mass"][:] = masses.astype(F32)
+        self.masses = masses.astype(F32).astype(np.float64)
+        return self.masses
+
+    def place(self, positions):
+        if self.cuda:
+            self.s.x.assign(positions)
+        else:
+            self.s.set("x", positions)
+
+    def x(self):
+        return self.s.x.numpy() if self.cuda else self.s.get("x")
+
+    def solve(self, velocity):
+        """test_blade_constraint.py:50-55: grid velocities set, reaction and torque cleared, one solve."""
+        s = self.s
+        if self.cuda:
+            s.new_v.assign(velocity.astype(F32))
+            s.reaction.zero_()
+            s.torque.zero_()
+            s.blade_constraint.solve()
+            return s.new_v.numpy().astype(np.float64)
+        s.arrays["new_v"][:] = velocity.astype(F32)
+        s.arrays["acc"][:] = 0
+        s.hold_solve()
+        return s.arrays["new_v"].astype(np.float64)
+
+    def advecting(self, velocity):
+        return np.sum(self.weights[:, :, None] * velocity[self.slots], axis=1)
+
+    def reaction(self):
+        return (self.s.reaction.numpy() if self.cuda else self.s.get("reaction"))[0].astype(np.float64)
+
+    def torque(self):
+        return (self.s.torque.numpy() if self.cuda else self.s.get("torque"))[0].astype(np.float64)
+
+    def acc_words(self):
+        return self.s._t["acc"].cpu().numpy().view(np.uint64) if self.cuda else self.s.arrays["acc"].copy()
+
+    def errors(self):
+        return self.s.errors.numpy() if self.cuda else self.s.arrays["errors"]
+
+
+def shared_cut_fields(h):
+    """test_blade_constraint.py:56-119: four particles at the two broad faces of the held knife move
+    into it; after the solve they stop (no restitution), only the normal velocity changes, the
+    material impulse balances the reaction and its torque, energy does not grow, and neither the
+    particles nor the held knife move.  Returns what the solve produced, per particle corner."""
+    coupling = np.array([0.4, -0.2, 0.3, 1.0, -0.5, 0.7], F32)
+    h.tool(vel=[-0.07, 0.02, 0.01], omega=[0.1, 0.2, -0.3],
+           mobility=np.diag([2.0, 3.0, 4.0, 10.0, 12.0, 8.0]) + np.outer(coupling, coupling))
+    held = h.held_state()
+    # codes 1 and 2 are separated; the uncut field 0 is compatible with both
+    codes = np.repeat([0, 1, 2], [16, 24, 24])
+    assert len(codes) == h.n
+    masses = h.shared_grid(codes)
+    positions = np.full((h.n, 3), 1.0, F32)
+    active, sides = np.array([16, 17, 40, 41]), np.array([1.0, 1.0, -1.0, -1.0])
+    positions[active] = np.column_stack([sides * SMALL.blade_half_size[0], np.full(4, 0.003), np.full(4, 0.002)])
+    h.place(positions)
+    # a realizable velocity: free momenta of the three fields, the common field exchanging with each cut one
+    field_mass = np.array([16, 24, 24], np.float64) * h.mass / 8
+    free = field_mass[:, None] * np.array([[0.005, 0.03, 0.02], [-0.12, 0.03, 0.02], [0.08, 0.03, 0.02]])
+    momentum = free.copy()
+    for a, b in [(0, 1), (0, 2)]:
+        exchange = (field_mass[a] * free[b] - field_mass[b] * free[a]) / field_mass.sum()
+        momentum[a] += exchange
+        momentum[b] -= exchange
+    before = np.zeros((len(masses), 3))
+    for code in range(3):
+        before[np.unique(h.slots[codes == code])] = momentum[code] / field_mass[code]
+    before = before.astype(F32).astype(np.float64)
+    assert np.all(sides * h.advecting(before)[active, 0] < -0.03)
+
+    after = h.solve(before)
+    final = h.advecting(after)[active]
+    assert np.min(sides * final[:, 0]) >= -2e-6
+    assert np.max(np.abs(final[:, 0])) < 2e-6
+    np.testing.assert_allclose(after[:, 1:], before[:, 1:], atol=2e-8)
+    impulse = np.sum(masses[:, None] * (after - before), axis=0)
+    assert abs(impulse[0]) > 1e-5
+    np.testing.assert_allclose(impulse + h.reaction(), 0, atol=2e-9)
+    np.testing.assert_allclose(h.torque(), -np.cross([0.0, 0.003, 0.002], impulse), atol=2e-10)
+    assert 0.5 * np.sum(masses[:, None] * after**2) <= 0.5 * np.sum(masses[:, None] * before**2) + 1e-12
+    np.testing.assert_array_equal(h.x(), positions)
+    for name, value in h.held_state().items():
+        np.testing.assert_array_equal(value, held[name], err_msg=name)
+    assert not h.errors().any()
+    return [(after[h.slots], h.acc_words())]
+
+
+def entry_side(h):
+    """test_blade_constraint.py:122-166: a particle that entered from +x is still pushed back to +x
+    once it is past the midplane; leaving around the finite y edge clears the side (the solve then
+    changes nothing); re-entering from -x and crossing the other way pushes it back to -x."""
+    masses = h.shared_grid(np.zeros(h.n, np.int64))
+    positions = np.full((h.n, 3), 1.0, F32)
+    before = np.zeros((len(masses), 3))
+    occupied = masses > 0
+    half_x, half_y, _ = SMALL.blade_half_size
+    out = []
+
+    positions[0] = [half_x, 0, 0]
+    h.place(positions)
+    before[occupied, 0] = -0.1
+    h.solve(before)
+    positions[0, 0] = -0.0001
+    h.place(positions)
+    after = h.solve(before)
+    assert h.advecting(after)[0, 0] >= -2e-6
+    assert h.reaction()[0] < 0
+    out.append((after[h.slots], h.acc_words()))
+
+    positions[0] = [-half_x, half_y + 0.001, 0]
+    h.place(positions)
+    before[occupied, 0] = 0.1
+    outside = h.solve(before)
+    np.testing.assert_allclose(outside, before, atol=2e-8)
+    np.testing.assert_array_equal(h.reaction(), 0)
+    out.append((outside[h.slots], h.acc_words()))
+
+    positions[0] = [-half_x, 0, 0]
+    h.place(positions)
+    h.solve(before)
+    positions[0, 0] = 0.0001
+    h.place(positions)
+    after = h.solve(before)
+    assert h.advecting(after)[0, 0] <= 2e-6
+    assert h.reaction()[0] > 0
+    impulse = np.sum(masses[:, None] * (after - before), axis=0)
+    np.testing.assert_allclose(impulse + h.reaction(), 0, atol=2e-9)
+    assert not h.errors().any()
+    out.append((after[h.slots], h.acc_words()))
+    return out
+
+
+def test_held_blade_stops_shared_cut_fields_without_virtual_motion_or_restitution():
+    shared_cut_fields(Held())
+
+
+def test_entry_side_survives_midplane_crossing_and_resets_after_finite_edge_exit():
+    entry_side(Held())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene", [shared_cut_fields, entry_side])
+def test_gpu_solve_alone_matches_oracle(scene):
+    # the same scenes on the CUDA solver: the reference's assertions hold there too, and every particle
+    # corner's grid velocity and the fixed-point reaction and torque words equal the oracle's
+    for (v_gpu, acc_gpu), (v_cpu, acc_cpu) in zip(scene(Held(cuda=True)), scene(Held())):
+        np.testing.assert_array_equal(v_gpu, v_cpu)
+        np.testing.assert_array_equal(acc_gpu, acc_cpu)
