@@ -258,3 +258,24 @@ def test_single_field_baseline_bitexact():
         c.step(target_edge=(0.0, 0.0, 0.2), cutting=False)
     assert_same(g, c)
     assert g.v.numpy()[~left, 0].mean() < -0.01
+
+
+@pytest.mark.parametrize("mode", ["list", "hash"])
+def test_pair_search_far_outside_the_block_matches_oracle(mode):
+    # tests/test_hash_grid.py:15-28 restated for the pair search (the oracle's pair set is pinned by brute
+    # force in test_oracle_known_answers.py): three clusters 2-5 m outside the block, about 11,700 pairs
+    # in contact; every particle's pair impulse and the pair count equal the oracle's
+    g, c = both(replace(Config(), pair_search=mode))
+    rng = np.random.default_rng(45)
+    n = g.n
+    x = np.vstack([rng.normal(ctr, 0.004, (k, 3)) for ctr, k in
+                   zip([(2, 3, 4), (-2, 0, -3), (0.1, 0, 0.2)], [n // 3, n // 3, n - 2 * (n // 3)])]).astype(np.float32)
+    ref = np.column_stack([np.arange(n) * 0.02, np.zeros(n), np.zeros(n)]).astype(np.float32)
+    codes = np.where(np.arange(n) % 2 == 0, 1, 2).astype(np.int64)
+    g.x.assign(x), g.ref.assign(ref), g.codes.assign(codes)
+    c.set("x", x), c.set("ref", ref), c.set("codes", codes)
+    g.particle_contacts()
+    c.particle_contacts()
+    np.testing.assert_array_equal(g.impulses.numpy(), c.get("impulses"))
+    assert g.pair_count[1].numpy()[0] == c.arrays["pair_count"][1] > 10000
+    assert g.errors.numpy().tolist() == c.get("errors").tolist() == [0, 0, 0]

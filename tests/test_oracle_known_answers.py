@@ -519,3 +519,36 @@ def test_interval_accumulation_matches_single_substeps():
     np.testing.assert_allclose(angular, sum(p[1] for p in pieces), atol=2.0e-10)
     np.testing.assert_allclose(a.get("x"), b.get("x"), atol=1.0e-7)
     np.testing.assert_array_equal(a.get("codes"), b.get("codes"))
+
+
+def far_clusters(n, seed=45):
+    """tests/test_hash_grid.py:15-28 restated for the particle pair search: three clusters 2-5 m outside
+    the block, where hashed cells wrap (bucket wrap must not clip space).  Neighbouring particles carry
+    the incompatible codes 1 and 2 or reference positions 20 mm apart, so every pair within reach is a
+    contact."""
+    rng = np.random.default_rng(seed)
+    x = np.vstack([rng.normal(c, 0.004, (k, 3)) for c, k in
+                   zip([(2, 3, 4), (-2, 0, -3), (0.1, 0, 0.2)], [n // 3, n // 3, n - 2 * (n // 3)])]).astype(np.float32)
+    ref = np.column_stack([np.arange(n) * 0.02, np.zeros(n), np.zeros(n)]).astype(np.float32)
+    return x, ref, np.where(np.arange(n) % 2 == 0, 1, 2).astype(np.int64)
+
+
+def test_pair_search_far_outside_the_block_finds_every_pair():
+    # the pair list against brute force: every pair closer than the reach (2 radius at rest) by more
+    # than 1 um is found, and every found pair is within the reach plus 1 um
+    o = OracleSolver(Config())
+    x, ref, codes = far_clusters(o.n)
+    o.set("x", x), o.set("ref", ref), o.set("codes", codes)
+    o.particle_contacts()
+    new = (o.step_count + 1) % 2
+    keys = o.arrays["pair_keys"][new]
+    found = keys[keys >= 0]
+    assert len(found) == o.arrays["pair_count"][new] > 10000
+    xs = o.arrays["x"].astype(np.float64)  # device order, as the keys
+    d = np.linalg.norm(xs[:, None] - xs[None], axis=2)
+    reach = 2.0 * float(np.float32(o.params.radius))
+    inside = np.triu(d < reach - 1e-6, 1)
+    lo, hi = np.nonzero(inside)
+    assert set((lo * o.n + hi).tolist()) <= set(found.tolist())
+    assert np.all(d[found // o.n, found % o.n] < reach + 1e-6)
+    assert not o.arrays["errors"].any()
