@@ -12,7 +12,7 @@ whole scenes and reports the same errors.
 import numpy as np
 import pytest
 
-from oracle.fp64_scenes import freefall, triple_cut
+from oracle.fp64_scenes import block, freefall, triple_cut
 
 
 def test_float64_build_runs_the_same_scene():
@@ -50,3 +50,18 @@ def test_triple_cut_first_intervals_against_float64():
     assert r["interval_error_of_largest"]["max"] < 1e-3
     assert r["total"]["relative_error"] < 5e-3  # blade impulse within 0.5 %
     assert r["released_particles"]["float32"] == r["released_particles"]["float64"] > 0
+
+
+def test_knife_block_at_a_coarse_grid_against_float64_and_a_shifted_start():
+    # the 8-knife block at a 10 mm grid (12,800 particles), its first 0.2 ms with the knives pressing in:
+    # the float64 run, and a float32 run with the knives started 10 nm lower, both within 0.1 % on the
+    # knives' total impulse
+    r = block(substeps=20, window=10, spacing=0.01)
+    assert r["second_run"] == "float64" and r["largest_interval_impulse"] > 1e-4
+    assert r["total"]["relative_error"] < 1e-3
+    assert r["knife_position_difference_m"] < 1e-8
+    assert r["device_errors"]["float32"] == r["device_errors"]["float64"] == [0, 0, 0]
+    p = block(substeps=20, window=10, spacing=0.01, perturb=1e-8)
+    assert p["second_run"] == "float32, knives 1e-08 m lower"
+    assert p["total"]["relative_error"] < 1e-3
+    assert 0.0 < p["knife_position_difference_m"] < 2e-8
