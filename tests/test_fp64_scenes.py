@@ -2,11 +2,12 @@
 
 The CUDA path reproduces the float32 oracle bit for bit; the oracle's float64
 build (``OracleSolver(cfg, real=np.float64)``) runs the same restatement in
-double precision.  These tests run the leading part of two benchmark scenes
-in both and bound the float32 run's error on what the scenes report: the
-blade's impulse per coupling interval (blade force and impulse are held
-to 0.5 %) and the knife's pose.  ``oracle/fp64_scenes.py`` runs the
-whole scenes and reports the same errors.
+double precision.  These tests run the leading part of two benchmark scenes,
+and of the 8-knife block at a coarse grid, in both and bound the float32
+run's error on what the scenes report: the blade's impulse per coupling
+interval (blade force and impulse are held to 0.5 %) and the knife's pose.
+``oracle/fp64_scenes.py`` runs the whole scenes and reports the same errors,
+and compares a float32 run against one whose knives start 10 nm lower.
 """
 
 import numpy as np
