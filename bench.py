@@ -138,7 +138,7 @@ def traffic_per_launch(stage, n, slots):
     return float(data["bytes_per_particle"]) * n + float(data.get("bytes_per_slot", 0.0)) * slots
 
 
-def cpu_baseline(name, seconds=15.0, max_steps=None):
+def cpu_baseline(name, seconds=15.0, max_steps=None, warmup=1):
     from oracle.oracle import OracleSolver
 
     cfg, knives, velocity = workload(name)
@@ -146,7 +146,9 @@ def cpu_baseline(name, seconds=15.0, max_steps=None):
     o.set("tool_pos", knives)
     o.set("tool_vel", velocity)
     zero = np.zeros(3, np.float32)
-    o.step(zero, cutting=True)  # registration and first-touch outside the timing
+    warmup = max(1, warmup)
+    for _ in range(warmup):  # registration and first-touch outside the timing
+        o.step(zero, cutting=True)
     steps, begin = 0, time.perf_counter()
     while time.perf_counter() - begin < seconds and (max_steps is None or steps < max_steps):
         o.step(zero, cutting=True)
@@ -157,7 +159,8 @@ def cpu_baseline(name, seconds=15.0, max_steps=None):
         "unit": UNIT,
         "cores": o.num_threads(),
         "kind": "port",
-        "sample": f"{steps} substeps of the full {o.n}-particle workload after 1 untimed substep, C oracle with OpenMP",
+        "sample": f"{steps} substeps of the full {o.n}-particle workload after {warmup} untimed "
+                  f"substep{'s' if warmup > 1 else ''}, C oracle with OpenMP",
     }
 
 
@@ -620,7 +623,7 @@ def run_reference(args, rank, world):
     name = args.workload
     cfg, _, _ = workload(name)
     budget = max(10.0, min(120.0, 0.5 * (args.steps + args.warmup)))
-    base = cpu_baseline(name, seconds=budget, max_steps=args.steps)
+    base = cpu_baseline(name, seconds=budget, max_steps=args.steps, warmup=args.warmup)
     line = {
         "impl": "reference",
         "metric": METRIC,
