@@ -147,15 +147,17 @@ class Held:
         self.mass = float(F32(self.s.mass))
         self.tool(vel=[0, 0, 0], omega=[0, 0, 0], mobility=np.zeros((6, 6)))
 
-    def tool(self, vel, omega, mobility):
+    def tool(self, vel, omega, mobility, rot=(0.0, 0.0, 0.0, 1.0)):
         s = self.s
         if self.cuda:
             s.tool_pos.zero_()
+            s.tool_rot.assign([rot])
             s.tool_vel.assign([vel])
             s.tool_omega.assign([omega])
             s.tool_mobility.assign(np.asarray(mobility, F32))
         else:
             s.set("tool_pos", [0.0, 0.0, 0.0])
+            s.set("tool_rot", rot)
             s.set("tool_vel", vel)
             s.set("tool_omega", omega)
             s.set("mobility", np.asarray(mobility, F32))
@@ -225,14 +227,27 @@ class Held:
         return self.s.errors.numpy() if self.cuda else self.s.arrays["errors"]
 
 
-def shared_cut_fields(h):
+def turning(q):
+    """Rotation matrix of the float32 unit quaternion q (xyzw) as the knife holds it."""
+    x, y, z, w = np.asarray(q, F32).astype(np.float64) / np.linalg.norm(np.asarray(q, F32).astype(np.float64))
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def shared_cut_fields(h, turn=(0.0, 0.0, 0.0, 1.0), tangential=2e-8):
     """test_blade_constraint.py:56-119: four particles at the two broad faces of the held knife move
     into it; after the solve they stop (no restitution), only the normal velocity changes, the
     material impulse balances the reaction and its torque, energy does not grow, and neither the
-    particles nor the held knife move.  Returns what the solve produced, per particle corner."""
+    particles nor the held knife move.  Returns what the solve produced, per particle corner.
+
+    With `turn` (a unit quaternion, xyzw) the knife, the particles' offsets from it and the grid
+    velocities are all turned by it, and the assertions are taken in the knife's frame; the upright
+    scene (the reference's) turns by the identity, which changes no value."""
+    R = turning(turn)
     coupling = np.array([0.4, -0.2, 0.3, 1.0, -0.5, 0.7], F32)
     h.tool(vel=[-0.07, 0.02, 0.01], omega=[0.1, 0.2, -0.3],
-           mobility=np.diag([2.0, 3.0, 4.0, 10.0, 12.0, 8.0]) + np.outer(coupling, coupling))
+           mobility=np.diag([2.0, 3.0, 4.0, 10.0, 12.0, 8.0]) + np.outer(coupling, coupling), rot=turn)
     held = h.held_state()
     # codes 1 and 2 are separated; the uncut field 0 is compatible with both
     codes = np.repeat([0, 1, 2], [16, 24, 24])
@@ -240,7 +255,8 @@ def shared_cut_fields(h):
     masses = h.shared_grid(codes)
     positions = np.full((h.n, 3), 1.0, F32)
     active, sides = np.array([16, 17, 40, 41]), np.array([1.0, 1.0, -1.0, -1.0])
-    positions[active] = np.column_stack([sides * SMALL.blade_half_size[0], np.full(4, 0.003), np.full(4, 0.002)])
+    local = np.column_stack([sides * SMALL.blade_half_size[0], np.full(4, 0.003), np.full(4, 0.002)])
+    positions[active] = local @ R.T
     h.place(positions)
     # a realizable velocity: free momenta of the three fields, the common field exchanging with each cut one
     field_mass = np.array([16, 24, 24], np.float64) * h.mass / 8
@@ -253,18 +269,18 @@ def shared_cut_fields(h):
     before = np.zeros((len(masses), 3))
     for code in range(3):
         before[np.unique(h.slots[codes == code])] = momentum[code] / field_mass[code]
-    before = before.astype(F32).astype(np.float64)
-    assert np.all(sides * h.advecting(before)[active, 0] < -0.03)
+    before = (before @ R.T).astype(F32).astype(np.float64)
+    assert np.all(sides * (h.advecting(before) @ R)[active, 0] < -0.03)
 
     after = h.solve(before)
-    final = h.advecting(after)[active]
+    final = h.advecting(after)[active] @ R  # in the knife's frame
     assert np.min(sides * final[:, 0]) >= -2e-6
     assert np.max(np.abs(final[:, 0])) < 2e-6
-    np.testing.assert_allclose(after[:, 1:], before[:, 1:], atol=2e-8)
+    np.testing.assert_allclose((after @ R)[:, 1:], (before @ R)[:, 1:], atol=tangential)
     impulse = np.sum(masses[:, None] * (after - before), axis=0)
-    assert abs(impulse[0]) > 1e-5
+    assert abs((impulse @ R)[0]) > 1e-5
     np.testing.assert_allclose(impulse + h.reaction(), 0, atol=2e-9)
-    np.testing.assert_allclose(h.torque(), -np.cross([0.0, 0.003, 0.002], impulse), atol=2e-10)
+    np.testing.assert_allclose(h.torque() @ R, -np.cross([0.0, 0.003, 0.002], impulse @ R), atol=2e-10)
     assert 0.5 * np.sum(masses[:, None] * after**2) <= 0.5 * np.sum(masses[:, None] * before**2) + 1e-12
     np.testing.assert_array_equal(h.x(), positions)
     for name, value in h.held_state().items():
@@ -326,8 +342,23 @@ def test_entry_side_survives_midplane_crossing_and_resets_after_finite_edge_exit
     entry_side(Held())
 
 
+# 0.6 rad about (1, 2, 3)
+TURN = tuple(np.r_[np.sin(0.3) * np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0), np.cos(0.3)])
+
+
+def test_turned_knife_solves_the_turned_scene():
+    # the same four contacts with the whole scene turned: the reference's assertions hold in the knife's
+    # frame.  Turning the float32 grid velocities rounds each component by up to 6e-9 m/s, so the tangential
+    # components are held to 1e-7 instead of 2e-8.
+    shared_cut_fields(Held(), turn=TURN, tangential=1e-7)
+
+
+def turned_shared_cut_fields(h):
+    return shared_cut_fields(h, turn=TURN, tangential=1e-7)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene", [shared_cut_fields, entry_side])
+@pytest.mark.parametrize("scene", [shared_cut_fields, turned_shared_cut_fields, entry_side])
 def test_gpu_solve_alone_matches_oracle(scene):
     # the same scenes on the CUDA solver: the reference's assertions hold there too, and every particle
     # corner's grid velocity and the fixed-point reaction and torque words equal the oracle's
