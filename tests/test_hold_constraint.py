@@ -289,44 +289,51 @@ def shared_cut_fields(h, turn=(0.0, 0.0, 0.0, 1.0), tangential=2e-8):
     return [(after[h.slots], h.acc_words())]
 
 
-def entry_side(h):
+def entry_side(h, turn=(0.0, 0.0, 0.0, 1.0)):
     """test_blade_constraint.py:122-166: a particle that entered from +x is still pushed back to +x
     once it is past the midplane; leaving around the finite y edge clears the side (the solve then
-    changes nothing); re-entering from -x and crossing the other way pushes it back to -x."""
+    changes nothing); re-entering from -x and crossing the other way pushes it back to -x.  With
+    `turn` the knife, the particle's offset and the grid velocities are turned as in
+    shared_cut_fields, and the assertions are taken in the knife's frame."""
+    R = turning(turn)
+    h.tool(vel=[0, 0, 0], omega=[0, 0, 0], mobility=np.zeros((6, 6)), rot=turn)
     masses = h.shared_grid(np.zeros(h.n, np.int64))
     positions = np.full((h.n, 3), 1.0, F32)
-    before = np.zeros((len(masses), 3))
     occupied = masses > 0
     half_x, half_y, _ = SMALL.blade_half_size
     out = []
 
-    positions[0] = [half_x, 0, 0]
-    h.place(positions)
-    before[occupied, 0] = -0.1
+    def put(local):
+        positions[0] = R @ np.asarray(local, np.float64)
+        h.place(positions)
+
+    def moving(speed_x):
+        velocity = np.zeros((len(masses), 3))
+        velocity[occupied, 0] = speed_x
+        return (velocity @ R.T).astype(F32).astype(np.float64)
+
+    put([half_x, 0, 0])
+    before = moving(-0.1)
     h.solve(before)
-    positions[0, 0] = -0.0001
-    h.place(positions)
+    put([-0.0001, 0, 0])
     after = h.solve(before)
-    assert h.advecting(after)[0, 0] >= -2e-6
-    assert h.reaction()[0] < 0
+    assert (h.advecting(after) @ R)[0, 0] >= -2e-6
+    assert (h.reaction() @ R)[0] < 0
     out.append((after[h.slots], h.acc_words()))
 
-    positions[0] = [-half_x, half_y + 0.001, 0]
-    h.place(positions)
-    before[occupied, 0] = 0.1
+    put([-half_x, half_y + 0.001, 0])
+    before = moving(0.1)
     outside = h.solve(before)
     np.testing.assert_allclose(outside, before, atol=2e-8)
     np.testing.assert_array_equal(h.reaction(), 0)
     out.append((outside[h.slots], h.acc_words()))
 
-    positions[0] = [-half_x, 0, 0]
-    h.place(positions)
+    put([-half_x, 0, 0])
     h.solve(before)
-    positions[0, 0] = 0.0001
-    h.place(positions)
+    put([0.0001, 0, 0])
     after = h.solve(before)
-    assert h.advecting(after)[0, 0] <= 2e-6
-    assert h.reaction()[0] > 0
+    assert (h.advecting(after) @ R)[0, 0] <= 2e-6
+    assert (h.reaction() @ R)[0] > 0
     impulse = np.sum(masses[:, None] * (after - before), axis=0)
     np.testing.assert_allclose(impulse + h.reaction(), 0, atol=2e-9)
     assert not h.errors().any()
@@ -347,18 +354,23 @@ TURN = tuple(np.r_[np.sin(0.3) * np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0), np.c
 
 
 def test_turned_knife_solves_the_turned_scene():
-    # the same four contacts with the whole scene turned: the reference's assertions hold in the knife's
-    # frame.  Turning the float32 grid velocities rounds each component by up to 6e-9 m/s, so the tangential
+    # the same contacts with the whole scene turned: the reference's assertions hold in the knife's frame.
+    # Turning the float32 grid velocities rounds each component by up to 6e-9 m/s, so the tangential
     # components are held to 1e-7 instead of 2e-8.
     shared_cut_fields(Held(), turn=TURN, tangential=1e-7)
+    entry_side(Held(), turn=TURN)
 
 
 def turned_shared_cut_fields(h):
     return shared_cut_fields(h, turn=TURN, tangential=1e-7)
 
 
+def turned_entry_side(h):
+    return entry_side(h, turn=TURN)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene", [shared_cut_fields, turned_shared_cut_fields, entry_side])
+@pytest.mark.parametrize("scene", [shared_cut_fields, turned_shared_cut_fields, entry_side, turned_entry_side])
 def test_gpu_solve_alone_matches_oracle(scene):
     # the same scenes on the CUDA solver: the reference's assertions hold there too, and every particle
     # corner's grid velocity and the fixed-point reaction and torque words equal the oracle's
