@@ -21,6 +21,9 @@ bit-exactly with the oracle on the same inputs:
   matter, mirrored knives move alike and label their own digits, a knife
   beside the block falls freely, each knife pays its own cutting work
   (tests/test_multi_tool.py:21-106);
+* two or three knives crossing and turning over the same particles give
+  each knife exactly its lone contact, in every slot order
+  (tests/test_stress_replays.py:95-107);
 * the paper's cutting resistance stops growing with the cutting energy,
   while held particles make the force grow with it
   (tests/test_cut_resistance.py:74-111);
@@ -476,6 +479,123 @@ def test_each_knife_pays_its_own_cutting_work(first):
     assert c.get("tool_damage")[1 - first][0] == 1
     c.set_cut(2)
     assert not c.get("tool_damage").any()
+
+
+def turn(v):
+    """Unit quaternion (xyzw) of the rotation vector v."""
+    v = np.asarray(v, float)
+    a = np.linalg.norm(v)
+    return np.r_[np.sin(a / 2) * v / a, np.cos(a / 2)] if a > 0 else np.array([0.0, 0.0, 0.0, 1.0])
+
+
+def compose(a, b):
+    """Hamilton product a * b of xyzw quaternions."""
+    (ax, ay, az, aw), (bx, by, bz, bw) = a, b
+    return np.array([aw * bx + ax * bw + ay * bz - az * by, aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw, aw * bw - ax * bx - ay * by - az * bz])
+
+
+SHARED = np.array([[0.0007, -0.004, 0.039], [-0.0007, 0.003, 0.039], [0.0004, 0.006, 0.0388], [0.0002, -0.006, 0.0392]])
+
+
+class Knives:
+    """The contact probe of scripts/stress_multi_tool.py:46-117 on the oracle: four particles that every
+    knife touches (the rest of the block parked 10 m up, where only gravity acts), and one contact pass
+    (blade, board and cut damage) per call with the knives' state set and the interval sums cleared."""
+
+    def __init__(self, cfg):
+        self.o = o = OracleSolver(cfg)
+        x = np.column_stack([10 + 0.01 * np.arange(o.n), np.zeros(o.n), np.full(o.n, 10.0)])
+        x[:4] = SHARED
+        o.set("x", x.astype(np.float32))
+        self.count = cfg.tool_count
+
+    def contact(self, p, v, q, w, cutting, cut_index):
+        o, A = self.o, self.o.arrays
+        o.set_cut(cut_index)
+        o.set("tool_pos", p), o.set("tool_vel", v), o.set("tool_rot", q), o.set("tool_omega", w)
+        A["acc"][:] = 0
+        A["speed"][:] = 0
+        o.rigid_contacts(o.cut_bits(cutting))
+        return dict(damage=A["damage"][:, o.rank][:, :4].copy(),
+                    friction=A["histories"][1 : 1 + self.count][:, o.rank][:, :4].copy(),
+                    reaction=o.get("reaction").copy(), torque=o.get("torque").copy(),
+                    impulses=o.get("impulses").astype(float), board=o.get("board").copy(), work=o.get("work").copy())
+
+
+@pytest.mark.parametrize("seed", [0, 17, 913])
+@pytest.mark.parametrize("count", [2, 3])
+def test_simultaneous_rotating_crossings_preserve_independent_contacts(seed, count):
+    # tests/test_stress_replays.py:95-107 with scripts/stress_multi_tool.py:289-418 (motion "crossing"):
+    # two or three free knives cross each other and turn while cutting the same four particles.  In every
+    # slot order each knife's damage, friction history, reaction and torque equal that knife's contact
+    # alone; the particles' impulses and the cutting work are the single knives' sums; momentum balances.
+    from itertools import permutations
+
+    rng = np.random.default_rng(seed)
+    cfg = Config(free_blade=True, tool_count=count, cutting_energy=80.0)
+    poses = np.tile([0.0, 0.0, 0.06], (count, 1))
+    poses[:, 0] = np.linspace(-0.0003, 0.0003, count)
+    velocities = rng.uniform(-0.08, 0.08, (count, 3))
+    velocities[:, 2] = -np.linspace(0.25, 0.65, count)
+    omegas = rng.uniform(-0.3, 0.3, (count, 3))
+    rng.uniform(-0.004, 0.004, (count, 3))  # the fixed-motion rotations, drawn to keep the stream aligned
+    velocities[:, 0] = -2 * poses[:, 0] / (9 * cfg.dt)
+    omegas[:, 2] += np.linspace(8.0, -8.0, count)
+    rotations = np.array([turn([0, 0, a]) for a in np.linspace(-0.08, 0.08, count)])
+    baseline = None
+    for order in map(np.asarray, permutations(range(count))):
+        inverse = np.argsort(order)
+        together, alone = Knives(cfg), [Knives(replace(cfg, tool_count=1)) for _ in order]
+        gravity = np.array([0.0, 0.0, -9.81 * float(np.float32(together.o.mass)) * float(np.float32(cfg.dt))])
+        trace = []
+        for tick in range(12):
+            p, v, w = poses.copy(), velocities.copy(), omegas.copy()
+            elapsed = (tick - min(2, max(0, tick - 5))) * cfg.dt
+            p[:, 0] += velocities[:, 0] * elapsed
+            q = np.array([compose(turn(omega * elapsed), r) for omega, r in zip(omegas, rotations)])
+            if tick in (3, 4):
+                p[0, 0] += 0.2  # one knife leaves; the others keep their histories
+            if tick in (6, 7):
+                v[:] = w[:] = 0.0
+            if tick >= 8:
+                v[:, 1] *= -1
+            cutting, cut_index = tick not in (6, 7), count if tick >= 9 else 0
+            state = together.contact(p[order], v[order], q[order], w[order], cutting, cut_index)
+            singles = [k.contact(p[i : i + 1], v[i : i + 1], q[i : i + 1], w[i : i + 1], cutting, cut_index)
+                       for i, k in enumerate(alone)]
+            for key in ("damage", "friction", "reaction", "torque"):
+                state[key] = state[key][inverse]
+                np.testing.assert_allclose(state[key], np.concatenate([s[key] for s in singles]), rtol=2e-5,
+                                           atol=1e-9, err_msg=f"{key}, tick {tick}")
+            np.testing.assert_allclose(state["impulses"], sum(s["impulses"] for s in singles) - (count - 1) * gravity,
+                                       rtol=2e-5, atol=1e-9)
+            np.testing.assert_allclose(state["work"], sum(s["work"] for s in singles), rtol=2e-5, atol=1e-9)
+            residual = (state["impulses"].sum(0) + state["reaction"].sum(0) - together.o.n * gravity
+                        - state["board"].sum(0))
+            np.testing.assert_allclose(residual, 0, atol=1e-9)
+            if tick == 2:
+                assert np.all(state["damage"] > 0), "the knives must damage the same particles"
+                assert np.all(np.linalg.norm(state["friction"], axis=(1, 2)) > 0)
+                assert np.all(np.linalg.norm(state["torque"], axis=1) > 0)
+                assert not np.allclose(state["friction"][0], state["friction"][1], atol=1e-9)
+            if tick == 4:
+                np.testing.assert_array_equal(state["friction"][0], 0)
+                np.testing.assert_array_equal(state["reaction"][0], 0)
+                assert np.linalg.norm(state["friction"][1:]) > 0
+            if tick in (6, 7):
+                np.testing.assert_array_equal(state["damage"], trace[-1]["damage"])
+            trace.append(state)
+        if baseline is None:
+            baseline = trace
+        else:
+            for tick, (actual, first) in enumerate(zip(trace, baseline)):
+                for key in first:
+                    np.testing.assert_allclose(actual[key], first[key], rtol=2e-5, atol=1e-9,
+                                               err_msg=f"order {order}, tick {tick}, {key}")
+    crossed = sum((poses[a, 0] - poses[b, 0]) * (p[a, 0] - p[b, 0]) < 0 for a in range(count) for b in range(a + 1, count))
+    assert crossed == count * (count - 1) // 2
+    assert np.max(2 * np.arccos(np.clip(np.abs(np.sum(q * rotations, axis=1)), 0, 1))) > 0.03
 
 
 # -------------------------------------------------------- cutting resistance
