@@ -21,9 +21,9 @@ bit-exactly with the oracle on the same inputs:
   matter, mirrored knives move alike and label their own digits, a knife
   beside the block falls freely, each knife pays its own cutting work
   (tests/test_multi_tool.py:21-106);
-* two or three knives crossing and turning over the same particles give
-  each knife exactly its lone contact, in every slot order
-  (tests/test_stress_replays.py:95-107);
+* two or three knives, fixed or crossing and turning, over the same
+  particles give each knife exactly its lone contact, in every slot order
+  (tests/test_multi_tool.py:108-116, tests/test_stress_replays.py:95-107);
 * the paper's cutting resistance stops growing with the cutting energy,
   while held particles make the force grow with it
   (tests/test_cut_resistance.py:74-111);
@@ -523,13 +523,15 @@ class Knives:
                     impulses=o.get("impulses").astype(float), board=o.get("board").copy(), work=o.get("work").copy())
 
 
+@pytest.mark.parametrize("motion", ["fixed", "crossing"])
 @pytest.mark.parametrize("seed", [0, 17, 913])
 @pytest.mark.parametrize("count", [2, 3])
-def test_simultaneous_rotating_crossings_preserve_independent_contacts(seed, count):
-    # tests/test_stress_replays.py:95-107 with scripts/stress_multi_tool.py:289-418 (motion "crossing"):
-    # two or three free knives cross each other and turn while cutting the same four particles.  In every
-    # slot order each knife's damage, friction history, reaction and torque equal that knife's contact
-    # alone; the particles' impulses and the cutting work are the single knives' sums; momentum balances.
+def test_simultaneous_knives_preserve_independent_contacts(motion, seed, count):
+    # scripts/stress_multi_tool.py:289-418 as tests/test_multi_tool.py:108-116 ("fixed": the knives hold
+    # their places and reverse) and tests/test_stress_replays.py:95-107 ("crossing": they cross each other
+    # and turn) run it: two or three free knives cut the same four particles.  In every slot order each
+    # knife's damage, friction history, reaction and torque equal that knife's contact alone; the
+    # particles' impulses and the cutting work are the single knives' sums; momentum balances.
     from itertools import permutations
 
     rng = np.random.default_rng(seed)
@@ -539,10 +541,12 @@ def test_simultaneous_rotating_crossings_preserve_independent_contacts(seed, cou
     velocities = rng.uniform(-0.08, 0.08, (count, 3))
     velocities[:, 2] = -np.linspace(0.25, 0.65, count)
     omegas = rng.uniform(-0.3, 0.3, (count, 3))
-    rng.uniform(-0.004, 0.004, (count, 3))  # the fixed-motion rotations, drawn to keep the stream aligned
-    velocities[:, 0] = -2 * poses[:, 0] / (9 * cfg.dt)
-    omegas[:, 2] += np.linspace(8.0, -8.0, count)
-    rotations = np.array([turn([0, 0, a]) for a in np.linspace(-0.08, 0.08, count)])
+    rotations = np.array([turn(v) for v in rng.uniform(-0.004, 0.004, (count, 3))])
+    crossing = motion == "crossing"
+    if crossing:
+        velocities[:, 0] = -2 * poses[:, 0] / (9 * cfg.dt)
+        omegas[:, 2] += np.linspace(8.0, -8.0, count)
+        rotations = np.array([turn([0, 0, a]) for a in np.linspace(-0.08, 0.08, count)])
     baseline = None
     for order in map(np.asarray, permutations(range(count))):
         inverse = np.argsort(order)
@@ -550,16 +554,19 @@ def test_simultaneous_rotating_crossings_preserve_independent_contacts(seed, cou
         gravity = np.array([0.0, 0.0, -9.81 * float(np.float32(together.o.mass)) * float(np.float32(cfg.dt))])
         trace = []
         for tick in range(12):
-            p, v, w = poses.copy(), velocities.copy(), omegas.copy()
-            elapsed = (tick - min(2, max(0, tick - 5))) * cfg.dt
-            p[:, 0] += velocities[:, 0] * elapsed
-            q = np.array([compose(turn(omega * elapsed), r) for omega, r in zip(omegas, rotations)])
+            p, v, w, q = poses.copy(), velocities.copy(), omegas.copy(), rotations.copy()
+            if crossing:
+                elapsed = (tick - min(2, max(0, tick - 5))) * cfg.dt
+                p[:, 0] += velocities[:, 0] * elapsed
+                q = np.array([compose(turn(omega * elapsed), r) for omega, r in zip(omegas, rotations)])
             if tick in (3, 4):
                 p[0, 0] += 0.2  # one knife leaves; the others keep their histories
             if tick in (6, 7):
                 v[:] = w[:] = 0.0
             if tick >= 8:
                 v[:, 1] *= -1
+                if not crossing:
+                    v[:, 0] *= -1
             cutting, cut_index = tick not in (6, 7), count if tick >= 9 else 0
             state = together.contact(p[order], v[order], q[order], w[order], cutting, cut_index)
             singles = [k.contact(p[i : i + 1], v[i : i + 1], q[i : i + 1], w[i : i + 1], cutting, cut_index)
@@ -593,9 +600,11 @@ def test_simultaneous_rotating_crossings_preserve_independent_contacts(seed, cou
                 for key in first:
                     np.testing.assert_allclose(actual[key], first[key], rtol=2e-5, atol=1e-9,
                                                err_msg=f"order {order}, tick {tick}, {key}")
-    crossed = sum((poses[a, 0] - poses[b, 0]) * (p[a, 0] - p[b, 0]) < 0 for a in range(count) for b in range(a + 1, count))
-    assert crossed == count * (count - 1) // 2
-    assert np.max(2 * np.arccos(np.clip(np.abs(np.sum(q * rotations, axis=1)), 0, 1))) > 0.03
+    if crossing:
+        crossed = sum((poses[a, 0] - poses[b, 0]) * (p[a, 0] - p[b, 0]) < 0
+                      for a in range(count) for b in range(a + 1, count))
+        assert crossed == count * (count - 1) // 2
+        assert np.max(2 * np.arccos(np.clip(np.abs(np.sum(q * rotations, axis=1)), 0, 1))) > 0.03
 
 
 # -------------------------------------------------------- cutting resistance
