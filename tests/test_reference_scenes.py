@@ -24,6 +24,9 @@ bit-exactly with the oracle on the same inputs:
 * two or three knives, fixed or crossing and turning, over the same
   particles give each knife exactly its lone contact, in every slot order
   (tests/test_multi_tool.py:108-116, tests/test_stress_replays.py:95-107);
+* three free knives falling through the block over two strokes give the same
+  trajectories, damage, side codes and pieces in every slot order once the
+  knives and their digits are mapped back (tests/test_multi_tool.py:119-133);
 * the paper's cutting resistance stops growing with the cutting energy,
   while held particles make the force grow with it
   (tests/test_cut_resistance.py:74-111);
@@ -605,6 +608,100 @@ def test_simultaneous_knives_preserve_independent_contacts(motion, seed, count):
                       for a in range(count) for b in range(a + 1, count))
         assert crossed == count * (count - 1) // 2
         assert np.max(2 * np.arccos(np.clip(np.abs(np.sum(q * rotations, axis=1)), 0, 1))) > 0.03
+
+
+def canonical_codes(codes, order, strokes):
+    """scripts/stress_multi_tool.py:135-146: codes written with knife order[slot] in slot `slot`, rewritten
+    as if every knife sat in the slot of its own identity (each stroke owns len(order) digits)."""
+    codes = np.asarray(codes, dtype=np.int64)
+    count, out = len(order), np.zeros_like(codes)
+    if np.any(codes // 3 ** (strokes * count)):
+        raise AssertionError("Unexpected cut digit outside the replay history")
+    for stroke in range(strokes):
+        for slot, identity in enumerate(order):
+            out += (codes // 3 ** (stroke * count + slot)) % 3 * 3 ** (stroke * count + identity)
+    return out
+
+
+def test_permutation_maps_each_strokes_ternary_digits():
+    # tests/test_multi_tool.py:119-125: slot order C, A, B: [1,2,2; 1,1,2] becomes A, B, C: [2,2,1; 1,2,1]
+    np.testing.assert_array_equal(canonical_codes([619, 0], [2, 0, 1], 2), [449, 0])
+    with pytest.raises(AssertionError, match="Unexpected cut digit"):
+        canonical_codes([3**6], [2, 0, 1], 2)
+
+
+def test_three_knives_full_trajectory_and_cut_history_permutation():
+    # tests/test_multi_tool.py:128-133 with scripts/stress_multi_tool.py:422-537: three free knives fall
+    # into the block (two strokes of 60 substeps) in every slot order, and once again in the first order.
+    # After the knives and their cut digits are mapped back to their identities, every run equals the
+    # first within the reference's bounds (10 ppm of a cell in position, 5 ppm of a cell per step in
+    # velocity, 1e-4 in damage, 10 uN of force), side codes and pieces exactly; momentum balances
+    # each substep to 50 ppm of one substep's gravity impulse, and every knife cuts in both strokes.
+    from itertools import permutations
+
+    count, steps = 3, 120
+    cfg = Config(free_blade=True, tool_count=count, cache_topology=True, grid_storage="compact", dt=0.0005)
+    rng = np.random.default_rng(17)
+    poses = np.tile([0.0, 0.0, 0.052], (count, 1))
+    poses[:, 0] = np.linspace(-0.001, 0.001, count)
+    velocities = rng.uniform(-0.015, 0.015, (count, 3))
+    velocities[:, 2] = -np.linspace(0.4, 0.6, count)
+    omegas = rng.uniform(-0.1, 0.1, (count, 3))
+    rotations = np.array([turn(v) for v in rng.uniform(-0.005, 0.005, (count, 3))])
+    h, dt = cfg.grid_spacing, cfg.dt
+    speed, impulse = 5e-6 * h / dt, 1e-5 * dt
+    atol = dict(position=1e-5 * h, velocity=speed, deformation=5e-6, plastic_deformation=1e-7,
+                blade_position=1e-5 * h, blade_velocity=speed, blade_orientation=1e-7,
+                blade_omega=speed / float(np.linalg.norm(cfg.blade_half_size)), tool_damage=1e-4,
+                friction=1e-5 * h, reaction=impulse, torque=impulse * float(np.linalg.norm(cfg.blade_half_size)))
+    orders = list(permutations(range(count)))
+    baseline, shared = None, 0
+    for order in map(np.asarray, [orders[0], *orders]):
+        inverse = np.argsort(order)
+        o = OracleSolver(cfg)
+        o.set("tool_pos", poses[order]), o.set("tool_vel", velocities[order])
+        o.set("tool_rot", rotations[order]), o.set("tool_omega", omegas[order])
+        mass, total = float(o.mass), float(o.mass) * o.n + cfg.blade_mass * count
+        trace, old = [], np.zeros(o.n, np.int64)
+        previous_v, previous_blade = o.get("v").astype(float), o.get("tool_vel").astype(float)
+        for tick in range(steps):
+            o.step(cutting=True, cut_index=int(tick >= steps // 2) * count)
+            v, blade_v = o.get("v").astype(float), o.get("tool_vel").astype(float)
+            delta = mass * (v - previous_v).sum(0) + cfg.blade_mass * (blade_v - previous_blade).sum(0)
+            # the board's impulses of this substep on the particles and (table_impulse) on the knives
+            external = np.array([0.0, 0.0, -9.81 * total * dt]) + o.get("board").sum(0) + o.get("table_impulse").sum(0)
+            np.testing.assert_allclose(delta, external, atol=5e-5 * 9.81 * total * dt, rtol=0, err_msg=f"tick {tick}")
+            previous_v, previous_blade = v, blade_v
+            sides = canonical_codes(o.get("codes"), order, 2)
+            for digit in range(2 * count):  # a written digit never changes
+                before, now = (old // 3**digit) % 3, (sides // 3**digit) % 3
+                np.testing.assert_array_equal(now[before != 0], before[before != 0])
+            old = sides
+            labels, sizes = components(o.node_numpy, o.weight_numpy, sides)
+            state = dict(position=o.get("x").copy(), velocity=o.get("v").copy(), deformation=o.get("F").copy(),
+                         plastic_deformation=o.get("Fp").copy(), blade_position=o.get("tool_pos")[inverse].copy(),
+                         blade_velocity=o.get("tool_vel")[inverse].copy(),
+                         blade_orientation=o.get("tool_rot")[inverse].copy(),
+                         blade_omega=o.get("tool_omega")[inverse].copy(), tool_damage=o.get("tool_damage")[inverse].copy(),
+                         friction=o.arrays["histories"][1 : 1 + count][:, o.rank][inverse].copy(),
+                         reaction=o.get("reaction")[inverse], torque=o.get("torque")[inverse],
+                         sides=sides, component_labels=labels, component_sizes=sizes)
+            shared = max(shared, int(np.count_nonzero(np.sum(state["tool_damage"] > 0, axis=0) >= 2)))
+            trace.append(state)
+        for stroke in range(2):
+            for identity in range(count):
+                assert np.any((old // 3 ** (stroke * count + identity)) % 3), "missing cut history"
+        if baseline is None:
+            baseline = trace
+            continue
+        for tick, (actual, first) in enumerate(zip(trace, baseline)):
+            for key, value in first.items():
+                if key in atol:
+                    np.testing.assert_allclose(actual[key], value, rtol=0, atol=atol[key],
+                                               err_msg=f"order {order}, tick {tick}, {key}")
+                else:
+                    np.testing.assert_array_equal(actual[key], value, err_msg=f"order {order}, tick {tick}, {key}")
+    assert shared > 0, "no particle was cut by several knives"
 
 
 # -------------------------------------------------------- cutting resistance
