@@ -58,6 +58,20 @@ def test_gravity_knife_stable_step_stays_valid_on_the_oracle():
     assert o.get("tool_pos")[0, 2] < 0.08 + 0.02  # the edge is in the block
 
 
+def test_edge_height_and_tilt_follow_the_rotated_edge():
+    # tests/test_cut_resistance.py:114-120: the gravity knife's edge height is the lowest point of its
+    # edge; upright at 50 mm with a 30 mm half height it is 20 mm, turned flat about y it is the centre
+    from scipy.spatial.transform import Rotation
+
+    from oracle.fp64_scenes import tilt
+
+    half = (0.0005, 0.04, 0.03)
+    upright, flat = Rotation.identity().as_quat(), Rotation.from_euler("y", 90, degrees=True).as_quat()
+    assert scenes.edge_height([0.0, 0.0, 0.05], upright, half) == pytest.approx(0.05 - 0.03, abs=1e-12)
+    assert scenes.edge_height([0.0, 0.0, 0.0005], flat, half) == pytest.approx(0.0005, abs=1e-12)
+    assert tilt(upright) == pytest.approx(0.0, abs=1e-9) and tilt(flat) == pytest.approx(90.0, abs=1e-9)
+
+
 def test_triple_cut_keyframes():
     keys = scenes.triple_cut_keyframes()
     cuts = [k for k in keys if k[2] >= 0]
