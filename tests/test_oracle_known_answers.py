@@ -552,3 +552,41 @@ def test_pair_search_far_outside_the_block_finds_every_pair():
     assert set((lo * o.n + hi).tolist()) <= set(found.tolist())
     assert np.all(d[found // o.n, found % o.n] < reach + 1e-6)
     assert not o.arrays["errors"].any()
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_pair_recontact_reference_exclusion_and_equal_opposite_impulse(split):
+    # tests/test_mechanics.py:340-420: two particles 2 mm apart closing at 2 x (0.01, 0.003, 0) m/s, their
+    # reference positions where they are.  Split (codes 1 and 2) they contact with equal and opposite
+    # impulses, normal plus stick/slip friction, as a float64 statement of pair_at (contact.py:583-640)
+    # gives them; uncut (codes 0 and 0) the reference exclusion leaves them alone.  The rest of the block
+    # is parked 20 mm apart, out of reach.
+    o = OracleSolver(Config(grid_spacing=0.006, dt=0.00025))
+    n = o.n
+    x = np.column_stack([10 + 0.02 * np.arange(n), np.zeros(n), np.full(n, 10.0)])
+    x[:2] = [[0.0, 0.0, 0.05], [0.002, 0.0, 0.05]]
+    v = np.zeros((n, 3))
+    v[:2] = [[0.01, 0.003, 0.0], [-0.01, -0.003, 0.0]]
+    codes = np.zeros(n, np.int64)
+    codes[:2] = [1, 2] if split else [0, 0]
+    x, v = x.astype(F32), v.astype(F32)
+    o.set("x", x), o.set("ref", x), o.set("v", v), o.set("codes", codes), o.set("impulses", np.zeros((n, 3), F32))
+    o.arrays["speed"][:] = np.linalg.norm(v, axis=1).max()
+    o.particle_contacts()
+    out = o.get("impulses")[:2].astype(float)
+
+    p = o.params
+    r, dt, me = float(F32(p.radius)), float(F32(p.dt)), float(F32(p.mass)) / 2.0
+    delta = x[0].astype(float) - x[1].astype(float)
+    dist = np.linalg.norm(delta)
+    normal, relative = delta / dist, v[0].astype(float) - v[1].astype(float)
+    predicted = 2.0 * r - dist - dt * min(relative @ normal, 0.0)
+    jn = float(F32(p.normal_scale)) * me / dt * predicted
+    jt, _ = friction_fp64(normal, relative, jn, np.zeros(3), me, dt, float(F32(p.friction_static)),
+                          float(F32(p.friction_dynamic)), float(F32(p.tangent_stiffness)), float(F32(p.tangent_damping)))
+    expected = normal * jn + jt if split else np.zeros(3)
+    np.testing.assert_allclose(out, [expected, -expected], atol=1e-10)
+    np.testing.assert_allclose(out.sum(0), 0, atol=1e-12)
+    assert bool(np.any(out)) == split
+    assert o.arrays["pair_count"][(o.step_count + 1) % 2] == int(split)
+    assert not o.arrays["errors"].any()
