@@ -1,8 +1,9 @@
 """Nodal embedding of a cut surface (surface.py:825-993, surface_gpu.py:11-345).
 
 CPU: the host tent supports against brute force (tests/test_surface.py:364-378
-of the reference) and the oracle's affine exactness and one-sided nodes
-(tests/test_surface.py:83-106, 381-393).  GPU: bm_embed_nodes /
+of the reference), the oracle's affine exactness and one-sided nodes
+(tests/test_surface.py:83-106, 381-393) and its invalid empty support
+(tests/test_surface_gpu.py:81-89).  GPU: bm_embed_nodes /
 bm_embed_vertices against the float64 oracle within the reference's own
 GPU-vs-CPU tolerance (1e-12, tests/test_surface_gpu.py:20-83), with equal
 extension counts, and the affine and cut-face properties on the device.
@@ -80,6 +81,20 @@ def test_oracle_unassigned_node_follows_one_side():
     ok = np.isfinite(shift)
     assert ok.sum() > len(nodes) // 2
     np.testing.assert_allclose(shift[ok], 0.03, atol=1.0e-12)
+
+
+def test_empty_support_stays_invalid_instead_of_freezing_or_zeroing():
+    # tests/test_surface_gpu.py:81-89: code 1 opposes every particle (all carry code 2), so no node has
+    # support for it: the oracle's field is NaN everywhere, and the product refuses a negative code on the
+    # host before any device call
+    from blademaster_gb300.surface import _codes
+
+    ref, _, _ = points(SIZE, H, "block")
+    emb = oracle.Embedding(surface_nodes(), ref, H)
+    field = emb.field(ref.copy(), np.tile(np.eye(3), (len(ref), 1, 1)), np.full(len(ref), 2), 1)
+    assert np.isnan(field).all()
+    with pytest.raises(ValueError):
+        _codes(np.array([-1]), 1)
 
 
 # ------------------------------------------------------------------- GPU
