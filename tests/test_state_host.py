@@ -52,7 +52,7 @@ def test_state_adds_viscous_deformation_and_every_knifes_damage_when_they_apply(
     s = Snapshot(Config(free_blade=True, tool_count=3), maxwell=True)
     state = s.state()
     assert set(state) == KEYS | {"viscous_deformation", "tool_damage"}
-    np.testing.assert_allclose(state["viscous_deformation"], np.eye(3) + 0.01)
+    np.testing.assert_allclose(state["viscous_deformation"], np.broadcast_to(np.eye(3) + 0.01, (4, 3, 3)))
     np.testing.assert_allclose(state["tool_damage"][:, 0], [0.0, 0.1, 0.2])
 
 
