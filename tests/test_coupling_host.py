@@ -43,3 +43,34 @@ def test_tool_state_and_configuration_are_validated():
         replace(Config(), external_tool=True, pose_servo=True)
     ok = ToolState([0, 0, 0.1], [0, 0, 0, 1], [0, 0, -0.02], [0, 0, 0]).checked()
     assert ok.mobility.shape == (6, 6) and not ok.mobility.any()
+
+
+class NoDevice:
+    """A solver stand-in for the port's host checks: reaching the cut bookkeeping means the checks let
+    the call through to the device path."""
+
+    def __init__(self, **config):
+        self.config = replace(Config(), **config)
+
+    def _set_cut(self, cut_index):
+        raise AssertionError("the port went on to the device path")
+
+
+def test_port_refuses_bad_durations_and_states_before_any_device_work():
+    # tests/test_coupling.py:74-88 on the host: only an external-tool solver gets a port; durations that
+    # are not a positive whole number of substeps (at most 4096) and invalid tool states are refused
+    # before the interval touches the solver
+    from blademaster_gb300.coupling import ExternalToolPort
+
+    with pytest.raises(ValueError, match="external_tool"):
+        ExternalToolPort(NoDevice())
+    solver = NoDevice(external_tool=True)
+    port, dt = ExternalToolPort(solver), solver.config.dt
+    state = ToolState([0.001, 0.0, 0.132], [0, 0, 0, 1], [0.01, 0.0, -0.02], [0.0, 0.1, 0.0])
+    for duration in [0.0, -1.0, np.nan, np.inf, 1.5 * dt, 4097 * dt]:
+        with pytest.raises(ValueError):
+            port.advance(state, duration)
+    with pytest.raises(ValueError, match="quaternion"):
+        port.advance(ToolState([0, 0, 0], [0, 0, 0, 2], [0, 0, 0], [0, 0, 0]), dt)
+    with pytest.raises(AssertionError, match="device path"):
+        port.advance(state, 4 * dt)  # a valid interval goes on
