@@ -118,3 +118,24 @@ def test_malformed_advance_orientation_preserves_previous_cut_history(orientatio
         probe.advance([[0, 0, 0.041]], cut_index=1, graph=False, orientations=orientations)
     assert probe.cut_index == 0 and probe.dispatched == []
     np.testing.assert_array_equal(probe.damage.numpy(), [0.75])
+
+
+@pytest.mark.parametrize("targets", [[], [[0, 0]], [[0, 0, float("nan")]], [[0, 0, float("inf")]], [0, 0, 0.041]])
+def test_malformed_advance_targets_preserve_previous_cut_history(targets):
+    # solver.py:942-973: targets must be finite (substeps, 3) edge positions, refused before the cut moves
+    probe = HostOnly()
+    probe.damage.fill_(0.75)
+    with pytest.raises(ValueError, match="targets"):
+        probe.advance(targets, cut_index=1, graph=False)
+    assert probe.cut_index == 0 and probe.dispatched == []
+    np.testing.assert_array_equal(probe.damage.numpy(), [0.75])
+
+
+def test_externally_owned_tool_refuses_the_solvers_own_stepping():
+    # tests/test_coupling.py:74-79 on the host
+    probe = HostOnly(Config(external_tool=True))
+    with pytest.raises(ValueError, match="ExternalToolPort"):
+        probe.step()
+    with pytest.raises(ValueError, match="ExternalToolPort"):
+        probe.advance([[0.0, 0.0, 0.0]])
+    assert probe.dispatched == [] and probe.cut_index == 0
